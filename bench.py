@@ -1,0 +1,347 @@
+"""Benchmark: forward NTT, n = 2^24, BabyBear, on GB300 (one JSON line).
+
+Contract: `python bench.py --gpus N --steps K --warmup W` (N > 1 under
+torchrun, one rank per GPU; replicas of the same workload, weak scaling).
+`--impl reference` times the reference algorithm's CPU implementation on the
+host cores instead (the C restatement of WinterfellFourStep, the reference's
+parallel full-NTT path; the Rust crate itself cannot be built here).
+
+A step = one forward NTT of 2^24 BabyBear words (u32), inputs resident in
+HBM.  The 64 MiB working set fits in L2, so L2 is flushed (a 256 MiB write)
+before every timed step, outside the timed events.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "omr-ntt_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Gelem/s & %HBM roofline, n=2^24 NTT"
+UNIT = "Gelem/s"
+LOG_N = 24
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--field", default="BabyBear")
+    ap.add_argument("--log-n", type=int, default=LOG_N)
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                smax = float(r[1])
+                for nm, v in zip(names, r[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(field, log_n, seconds, steps=None):
+    """The oracle's WinterfellFourStep (the reference's parallel four-step,
+    restated in C with OpenMP) on all host cores; bounded sample."""
+    import numpy as np
+    from oracle import oracle
+
+    oracle.set_threads(0)
+    cores = oracle.get_threads()
+    n = 1 << log_n
+    x = __import__("omr_ntt").gen_input_seeded(field, n, 42)
+    oracle.ntt(field.id, x, "WinterfellFourStep")  # warm-up (page-in)
+    times = []
+    t_end = time.perf_counter() + seconds
+    while (steps is None and (time.perf_counter() < t_end or not times)) or (steps is not None and len(times) < steps):
+        t0 = time.perf_counter()
+        oracle.ntt(field.id, x, "WinterfellFourStep")
+        times.append(time.perf_counter() - t0)
+    return n * len(times) / sum(times) / 1e9, cores, len(times), times
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    from omr_ntt.fields import field_by_name
+
+    field = field_by_name(args.field)
+    n = 1 << args.log_n
+    cpu_baseline(field, args.log_n, 0, steps=max(1, args.warmup))
+    val, cores, cnt, times = cpu_baseline(field, args.log_n, 0, steps=args.steps)
+    ms = 1000 * sum(times) / len(times)
+    sample = (f"{cnt} x WinterfellFourStep {field.name} n=2^{args.log_n} forward (C restatement of "
+              f"src/encoders/winterfell_four_step.rs, OpenMP {cores} threads)")
+    line = {
+        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32" if field.word_bytes == 4 else "u64",
+        "data": "synthetic (splitmix64 seed 42, uniform [0,p))",
+        "config": {"workload": f"{field.name} forward NTT n=2^{args.log_n}, batch 1",
+                   "field": field.name, "log_n": args.log_n, "batch": 1},
+        "impl": "reference",
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    import omr_ntt
+    from omr_ntt import NttDomain, _lib
+    from omr_ntt.fields import BabyBear, Goldilocks, field_by_name
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    field = field_by_name(args.field)
+    log_n = args.log_n
+    n = 1 << log_n
+    w = field.word_bytes
+    sdt = torch.int32 if w == 4 else torch.int64
+    domain = NttDomain(field, n)
+    x = omr_ntt.gen_input_seeded(field, n, 42 + rank)
+    xd = torch.from_numpy(x.view(np.int32 if w == 4 else np.int64).copy()).cuda()
+    buf = xd.clone()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    L = _lib.lib()
+    plan = -1
+    passes = omr_ntt.plan_passes(field, log_n, plan)
+
+    def step():
+        _lib.check(L.omr_ntt_forward(domain.handle, plan, ctypes.c_void_p(buf.data_ptr()),
+                                     ctypes.c_void_p(buf.data_ptr()), 1, sp))
+
+    assert args.warmup >= 3, "need >= 3 warm-up steps"
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        for e0, e1 in evs:
+            flush.zero_()
+            e0.record(stream)
+            step()
+            e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = n * world * args.steps / (total_ms / 1e3) / 1e9
+    ms_per_step = total_ms / args.steps
+
+    # ---- per-pass timing (the dominant kernel's roofline), same stream, CUDA events
+    scratch = torch.empty_like(buf)
+    pass_ms = []
+    for pi in range(len(passes)):
+        ts = []
+        for _ in range(max(3, args.steps // 2)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _lib.check(L.omr_ntt_plan_run_pass(domain.handle, plan, pi, 0, ctypes.c_void_p(buf.data_ptr()),
+                                               ctypes.c_void_p(scratch.data_ptr()),
+                                               ctypes.c_void_p(buf.data_ptr()), 1, sp))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        pass_ms.append(sum(ts) / len(ts))
+    dom = max(range(len(pass_ms)), key=lambda i: pass_ms[i])
+    peak, peak_src = peaks()
+    alg_bytes = 2 * n * w  # one read + one write of the data per pass launch
+    achieved = alg_bytes / (pass_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath))
+        key = f"{field.name}:{log_n}:pass{dom}"
+        traffic = tj.get(key)
+
+    # ---- end to end through the C ABI with host buffers (pinned), copies inside
+    hbuf = torch.from_numpy(x.view(np.int32 if w == 4 else np.int64).copy()).pin_memory()
+    hp = ctypes.c_void_p(hbuf.data_ptr())
+    for _ in range(2):
+        _lib.check(L.omr_ntt_forward_host(domain.handle, plan, hp, 1))
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _lib.check(L.omr_ntt_forward_host(domain.handle, plan, hp, 1))
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_val = n * world * len(e2e_t) / sum(e2e_t) / 1e9
+
+    # ---- extras: other BASELINE config-2 shapes (a few steps each)
+    extras = {}
+    if not args.no_extras:
+        def timed(fn, reps=5):
+            for _ in range(2):
+                flush.zero_()
+                fn()
+            ts = []
+            for _ in range(reps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return sum(ts) / len(ts)
+
+        for fld, lg, bt, inv in ((BabyBear, 24, 1, True), (Goldilocks, 24, 1, False),
+                                 (Goldilocks, 24, 1, True), (BabyBear, 20, 64, False),
+                                 (Goldilocks, 20, 64, False), (BabyBear, 22, 1, False),
+                                 (BabyBear, 20, 1, False), (BabyBear, 27, 1, False)):
+            nn = 1 << lg
+            dd = NttDomain(fld, nn)
+            t = torch.empty(nn * bt, dtype=torch.int32 if fld.word_bytes == 4 else torch.int64, device="cuda")
+            t.random_(0, 1 << 30)
+            fn_ = L.omr_ntt_inverse if inv else L.omr_ntt_forward
+            ms = timed(lambda: _lib.check(fn_(dd.handle, -1, ctypes.c_void_p(t.data_ptr()),
+                                              ctypes.c_void_p(t.data_ptr()), bt, sp)))
+            gbs = 2 * nn * bt * fld.word_bytes / (ms / 1e3) / 1e9
+            extras[f"{fld.name} {'inv' if inv else 'fwd'} 2^{lg}x{bt}"] = {
+                "ms": round(ms, 4), "Gelem/s": round(nn * bt / (ms / 1e3) / 1e9, 2),
+                "GB/s_alg": round(gbs, 1), "frac_hbm": round(gbs / peak, 3)}
+            del t, dd
+
+    # ---- CPU baseline (rank 0, N=1 only): the oracle port on the host cores
+    cpu = None
+    if rank == 0 and world == 1:
+        cval, cores, cnt, _ = cpu_baseline(field, log_n, args.cpu_seconds)
+        cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cnt} x WinterfellFourStep {field.name} n=2^{log_n} forward, C restatement "
+                         f"of src/encoders/winterfell_four_step.rs, OpenMP {cores} threads"}
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32" if w == 4 else "u64",
+            "data": "synthetic (splitmix64 seed 42+rank, uniform [0,p))",
+            "config": {"workload": f"{field.name} forward NTT n=2^{log_n}, batch 1 per GPU",
+                       "field": field.name, "log_n": log_n, "batch": 1,
+                       "plan": omr_ntt.plan_describe(field, log_n, plan),
+                       "l2": "flushed (256 MiB write) before every timed step",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": f"ntt_tile_pass pass {dom} (logT={passes[dom]['logT']})",
+                         "peak_source": peak_src,
+                         "pass_ms": [round(t, 4) for t in pass_ms],
+                         "transform_frac": (2 * n * w / (ms_per_step / 1e3) / 1e9) / peak},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": n * w,
+                    "d2h_bytes_per_step": n * w,
+                    "path": "omr_ntt_forward_host (pinned host buffer, H2D + NTT + D2H + sync)"},
+            "gpu_launches": len(passes) * args.steps,
+            "clocks": clocks,
+            "extras": extras,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

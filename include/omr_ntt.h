@@ -1,0 +1,200 @@
+/*
+ * omr_ntt.h -- C ABI of the GB300 NTT engine (drop-in for the hot path of
+ * benbencik/omr-ntt).
+ *
+ * The reference crate's interface (Rust) is
+ *
+ *   pub struct NttDomain<F> { N, log_N, omega, twiddles, bitrev_twiddles }
+ *                                                   (src/encoder.rs:28-38)
+ *   NttDomain::<F>::new(N)                          (src/encoder.rs:42-70)
+ *   pub trait NttEncoder<F>: Send + Sync {
+ *       fn ntt(&self, buf: &mut [F], domain: &NttDomain<F>);
+ *       fn name(&self) -> &str;                     (src/encoder.rs:89-93)
+ *   }
+ *   encoders::all(log_n) / encoders::all_partial(s) (src/encoders/mod.rs:32-54)
+ *
+ * over the fields of src/fields.rs.  Each function below names the reference
+ * item it replaces.  Elements cross the ABI as canonical words: uint32_t for
+ * BabyBear, KoalaBear and TeddyBear, uint64_t for Goldilocks (a Rust shim
+ * converts ark-ff's Montgomery-form Fp to and from canonical integers).
+ *
+ * Errors: the reference panics through assert! (src/encoder.rs:43-51,
+ * src/encoders/lambdaworks_radix4.rs:17-21, tfhe_stockham_radix8.rs:17-21,
+ * transform_decomposition.rs:28); every function here returns an
+ * omr_ntt_status instead and leaves the caller's buffers untouched on a
+ * host-detected error.  omr_ntt_last_error() gives a one-line message.
+ *
+ * Device functions take device pointers and a cudaStream_t passed as void*
+ * (NULL = legacy default stream) and are asynchronous.  *_host functions take
+ * host pointers, copy through device memory owned by the domain, and are
+ * synchronous.  Domains are thread-safe; scratch memory is owned by the domain
+ * and kept per stream.
+ */
+#ifndef OMR_NTT_H
+#define OMR_NTT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Fields (src/fields.rs:4-19). */
+typedef enum {
+  OMR_NTT_BABYBEAR = 0,   /* p = 2^31 - 2^27 + 1, generator 31, 2-adicity 27 (DefaultField) */
+  OMR_NTT_GOLDILOCKS = 1, /* p = 2^64 - 2^32 + 1, generator 7,  2-adicity 32 */
+  OMR_NTT_KOALABEAR = 2,  /* p = 2^31 - 2^24 + 1, generator 3,  2-adicity 24 */
+  OMR_NTT_TEDDYBEAR = 3   /* p = 2^32 - 2^30 + 1, generator 5,  2-adicity 30 */
+} omr_ntt_field;
+
+typedef enum {
+  OMR_NTT_OK = 0,
+  OMR_NTT_ERR_INVALID_ARGUMENT = -1, /* null handle/pointer, unknown id, bad count */
+  OMR_NTT_ERR_SIZE = -2,             /* N not a power of two, or log2 N > 2-adicity */
+  OMR_NTT_ERR_PRECONDITION = -3,     /* encoder precondition (radix-4: log N even; radix-8: log N % 3 == 0) */
+  OMR_NTT_ERR_CUDA = -4,             /* a CUDA runtime call failed */
+  OMR_NTT_ERR_ALLOC = -5,            /* device or host allocation failed */
+  OMR_NTT_ERR_TIMEOUT = -6,          /* a bounded device-side wait gave up */
+  OMR_NTT_ERR_NONCANONICAL = -7,     /* an input word is >= p (checked entry points only) */
+  OMR_NTT_ERR_DUPLICATE = -8,        /* an index set repeats an index */
+  OMR_NTT_ERR_CAPACITY = -9          /* a batch/queue capacity was exceeded */
+} omr_ntt_status;
+
+/* Encoders: the reference's registry (src/encoders/mod.rs:17-25).  Every
+ * encoder computes the same natural-order transform; on the GPU the id
+ * selects the plan family, and OMR_NTT_AUTO lets the planner choose. */
+typedef enum {
+  OMR_NTT_AUTO = -1,
+  OMR_NTT_ARK_RADIX2 = 0,               /* src/encoders/ark_radix2.rs:12-19 */
+  OMR_NTT_DFT = 1,                      /* src/encoders/dft.rs:9-22 */
+  OMR_NTT_DFT_PARTIAL = 2,              /* src/encoders/dft.rs:30-89 */
+  OMR_NTT_LAMBDA_BOWERS = 3,            /* src/encoders/lambdaworks_bowers.rs:13-173 */
+  OMR_NTT_LAMBDA_RADIX4 = 4,            /* src/encoders/lambdaworks_radix4.rs:14-75 */
+  OMR_NTT_PLONKY3_LAYER_SPLIT = 5,      /* src/encoders/plonky3_radix2_layer_split.rs:18-97 */
+  OMR_NTT_TFHE_STOCKHAM_R8 = 6,         /* src/encoders/tfhe_stockham_radix8.rs:15-140 */
+  OMR_NTT_TRANSFORM_DECOMPOSITION = 7,  /* src/encoders/transform_decomposition.rs:10-97 */
+  OMR_NTT_TRANSFORM_DECOMPOSITION_V2 = 8, /* src/encoders/transform_decomposition_v2.rs:8-100 */
+  OMR_NTT_WINTERFELL_FOUR_STEP = 9      /* src/encoders/winterfell_four_step.rs:19-130 */
+} omr_ntt_encoder;
+
+/* Output index patterns for partial transforms.  PREFIX is the reference's
+ * semantics (the first m outputs, src/encoders/transform_decomposition.rs:30);
+ * STRIDED and INDICES have no reference path. */
+typedef enum {
+  OMR_NTT_PATTERN_PREFIX = 0,  /* outputs X[0..count) */
+  OMR_NTT_PATTERN_STRIDED = 1, /* outputs X[j * (N / count)], j < count; count a power of two */
+  OMR_NTT_PATTERN_INDICES = 2  /* outputs X[idx[j]], j < count, idx distinct and < N */
+} omr_ntt_pattern;
+
+typedef struct omr_ntt_domain_s *omr_ntt_domain_t;
+
+/* ---------------------------------------------------------------- domain */
+
+/* NttDomain::<F>::new(N) (src/encoder.rs:42-70) with N = 2^log_n.  Builds the
+ * device twiddle tables on the current CUDA device (setup, untimed in the
+ * reference's benches: benches/ntt_bench_n.rs:10). */
+int omr_ntt_domain_create(int field, uint32_t log_n, omr_ntt_domain_t *out);
+
+/* Drop of NttDomain: frees device tables and every per-stream scratch buffer. */
+int omr_ntt_domain_destroy(omr_ntt_domain_t d);
+
+/* NttDomain fields N, log_N, omega (src/encoder.rs:30-33); omega canonical. */
+int omr_ntt_domain_info(omr_ntt_domain_t d, int *field, uint64_t *n, uint32_t *log_n,
+                        uint64_t *omega);
+
+/* NttDomain::twiddles (bitrev == 0: omega^k, k < N) or bitrev_twiddles
+ * (bitrev != 0: omega^bitrev(i, log_N - 1), i < N/2) (src/encoder.rs:34-37,
+ * :56-62), copied to host memory `out` of N (resp. N/2) words. */
+int omr_ntt_domain_twiddles(omr_ntt_domain_t d, int bitrev, void *out);
+
+/* ---------------------------------------------------------------- encoders */
+
+/* NttEncoder::name (src/encoder.rs:92): the reference encoder's name, or NULL. */
+const char *omr_ntt_encoder_name(int encoder);
+
+/* Whether `encoder` accepts log_n (radix-4: even; radix-8: divisible by 3),
+ * mirroring the reference's registry filter (src/encoders/mod.rs:41-46). */
+int omr_ntt_encoder_supports(int encoder, uint32_t log_n);
+
+/* NttEncoder::ntt(&self, buf, domain) (src/encoder.rs:90) on a device buffer:
+ * in place on `batch` transforms of N words stored back to back.  Partial
+ * encoders (DftPartial, TransformDecomposition, TransformDecompositionV2) use
+ * `s` and write only buf[..min(2s, N)] of each transform, as the reference
+ * does; full encoders ignore `s`. */
+int omr_ntt_encode(omr_ntt_domain_t d, int encoder, uint64_t s, void *buf, uint64_t batch,
+                   void *stream);
+
+/* Same as omr_ntt_encode on a host buffer (host -> device -> host inside). */
+int omr_ntt_encode_host(omr_ntt_domain_t d, int encoder, uint64_t s, void *host_buf,
+                        uint64_t batch);
+
+/* ---------------------------------------------------------------- transforms */
+
+/* Forward NTT X[k] = sum_i x[i] omega^(ik), natural order in and out.
+ * `in` may equal `out` (in place).  `plan` is a plan id from
+ * omr_ntt_plan_* or -1 for the planner's choice.  Replaces the hot call
+ * encoder.ntt(&mut buf, &domain) of benches/ntt_bench_n.rs:18-24. */
+int omr_ntt_forward(omr_ntt_domain_t d, int plan, const void *in, void *out, uint64_t batch,
+                    void *stream);
+
+/* Inverse NTT x[i] = N^-1 sum_k X[k] omega^(-ik) (no reference counterpart). */
+int omr_ntt_inverse(omr_ntt_domain_t d, int plan, const void *in, void *out, uint64_t batch,
+                    void *stream);
+
+/* Host-buffer forms of the two calls above (synchronous). */
+int omr_ntt_forward_host(omr_ntt_domain_t d, int plan, void *host_buf, uint64_t batch);
+int omr_ntt_inverse_host(omr_ntt_domain_t d, int plan, void *host_buf, uint64_t batch);
+
+/* Partial-output forward NTT: out[j] = X[sel(j)] for j < count, where sel is
+ * the pattern (PREFIX / STRIDED / INDICES).  `indices` (device, uint32_t) is
+ * read only for INDICES.  `in` is not modified.  The reference's partial
+ * encoders (TransformDecomposition(s), src/encoders/transform_decomposition.rs)
+ * are PREFIX with count = min(2s, N). */
+int omr_ntt_partial(omr_ntt_domain_t d, int pattern, uint64_t count, const uint32_t *indices,
+                    const void *in, void *out, void *stream);
+
+/* Host-buffer form of omr_ntt_partial (indices in host memory). */
+int omr_ntt_partial_host(omr_ntt_domain_t d, int pattern, uint64_t count,
+                         const uint32_t *indices, const void *in, void *out);
+
+/* Checked entry: returns OMR_NTT_ERR_NONCANONICAL if any input word >= p
+ * (device-side scan, one extra read of the input). */
+int omr_ntt_check_canonical(omr_ntt_domain_t d, const void *buf, uint64_t words, void *stream);
+
+/* ---------------------------------------------------------------- plans */
+
+/* Plans depend only on (field, log_n); these need no GPU.  A plan is a split
+ * of the transform into at most three tile passes (line lengths <= 4096).
+ * omr_ntt_plan_count returns the number of plans (or a negative status);
+ * omr_ntt_plan_describe writes a short name into `buf` (cap bytes). */
+int omr_ntt_plan_count(int field, uint32_t log_n);
+int omr_ntt_plan_describe(int field, uint32_t log_n, int plan, char *buf, size_t cap);
+
+/* Pass geometry of `plan` (-1: default) for `batch` transforms, for host-side
+ * checking: writes up to `cap` records of 16 uint64 words each and returns the
+ * pass count (or a negative status).  Layout of one record:
+ * [logT, L_lo, L_m, L_b, is_lo, is_m, is_b, os_lo, os_m, os_b, es_in, es_out,
+ *  twiddle(0/1), tw_scale, tw_line_mul_m, (in_buf | out_buf << 8)], with
+ * buffers 0 = source, 1 = scratch, 2 = destination. */
+int omr_ntt_plan_passes(int field, uint32_t log_n, int plan, uint64_t batch, uint64_t *records,
+                        int cap);
+
+/* Run pass `pass` (0-based) of `plan` alone, asynchronously on `stream`, with
+ * the pass's buffer roles bound to `src` (source), `scratch` (N * batch words,
+ * caller-owned) and `dst` (destination).  Running every pass in order equals
+ * omr_ntt_forward / omr_ntt_inverse; used to time and tune passes one at a
+ * time.  No reference counterpart (the reference has no pass structure). */
+int omr_ntt_plan_run_pass(omr_ntt_domain_t d, int plan, int pass, int inverse, const void *src,
+                          void *scratch, void *dst, uint64_t batch, void *stream);
+
+/* ---------------------------------------------------------------- misc */
+
+const char *omr_ntt_last_error(void);
+const char *omr_ntt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OMR_NTT_H */

@@ -1,0 +1,562 @@
+// engine.cu -- domain objects, device tables, pass plans, and the C ABI of
+// the full forward / inverse transforms.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+
+namespace omr {
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int two_adicity(int field) {
+  switch (field) {
+    case BABYBEAR: return BabyBear::TWO_ADICITY;
+    case GOLDILOCKS: return Goldilocks::TWO_ADICITY;
+    case KOALABEAR: return KoalaBear::TWO_ADICITY;
+    case TEDDYBEAR: return TeddyBear::TWO_ADICITY;
+  }
+  return -1;
+}
+
+uint64_t modulus(int field) {
+  switch (field) {
+    case BABYBEAR: return BabyBear::P;
+    case GOLDILOCKS: return Goldilocks::P;
+    case KOALABEAR: return KoalaBear::P;
+    case TEDDYBEAR: return TeddyBear::P;
+  }
+  return 0;
+}
+
+bool valid_field(int field) { return field >= 0 && field <= 3; }
+
+static uint64_t generator(int field) {
+  switch (field) {
+    case BABYBEAR: return BabyBear::GEN;
+    case GOLDILOCKS: return Goldilocks::GEN;
+    case KOALABEAR: return KoalaBear::GEN;
+    case TEDDYBEAR: return TeddyBear::GEN;
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------------ root tables
+static std::mutex g_roots_mu;
+static std::map<std::pair<int, int>, RootTables> g_roots;  // (device, field)
+
+template <class F>
+static int build_root_tables(RootTables* out) {
+  using Tw = typename F::Tw;
+  const uint64_t p = F::p64();
+  const uint64_t w = root_of_unity_host<F>(kMaxLogT);
+  const uint64_t wi = hpowmod(w, p - 2, p);
+  const int T = 1 << kMaxLogT;
+  std::vector<Tw> f(T), iv(T);
+  uint64_t a = 1, b = 1;
+  for (int k = 0; k < T; k++) {
+    f[k] = F::make_tw(a);
+    iv[k] = F::make_tw(b);
+    a = hmulmod(a, w, p);
+    b = hmulmod(b, wi, p);
+  }
+  void *df = nullptr, *di = nullptr;
+  OMR_CUDA_TRY(cudaMalloc(&df, sizeof(Tw) * T));
+  OMR_CUDA_TRY(cudaMalloc(&di, sizeof(Tw) * T));
+  OMR_CUDA_TRY(cudaMemcpy(df, f.data(), sizeof(Tw) * T, cudaMemcpyHostToDevice));
+  OMR_CUDA_TRY(cudaMemcpy(di, iv.data(), sizeof(Tw) * T, cudaMemcpyHostToDevice));
+  out->fwd = df;
+  out->inv = di;
+  return OMR_NTT_OK;
+}
+
+int get_root_tables(int field, RootTables* out) {
+  int dev = 0;
+  OMR_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_roots_mu);
+  auto key = std::make_pair(dev, field);
+  auto it = g_roots.find(key);
+  if (it != g_roots.end()) {
+    *out = it->second;
+    return OMR_NTT_OK;
+  }
+  RootTables rt;
+  int rc = with_field(field, [&](auto f) { return build_root_tables<decltype(f)>(&rt); });
+  if (rc) return rc;
+  g_roots[key] = rt;
+  *out = rt;
+  return OMR_NTT_OK;
+}
+
+// ------------------------------------------------------------------ plans
+std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
+  std::vector<PlanShape> out;
+  if (log_n == 0) {
+    out.push_back(PlanShape{{}});
+    return out;
+  }
+  int pmin = (int)((log_n + kMaxLogT - 1) / kMaxLogT);
+  if (pmin < 1) pmin = 1;
+  for (int P = pmin; P <= std::min(3, pmin + 1); P++) {
+    if ((uint32_t)P > log_n) break;
+    std::vector<int> s(P);
+    for (int i = 0; i < P; i++) s[i] = (int)(log_n / P) + (i < (int)(log_n % P) ? 1 : 0);
+    if (s[0] > kMaxLogT) continue;
+    out.push_back(PlanShape{s});
+    std::vector<int> r(s.rbegin(), s.rend());
+    if (r != s) out.push_back(PlanShape{r});
+  }
+  return out;
+}
+
+std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanShape& shape) {
+  std::vector<PassDesc> ps;
+  const uint64_t N = 1ull << log_n;
+  const int P = (int)shape.split.size();
+  auto base = [&](int logT) {
+    PassDesc d{};
+    d.logT = logT;
+    d.L_m = 1;
+    d.L_b = batch;
+    d.is_b = d.os_b = N;
+    d.is_m = d.os_m = 0;
+    d.twiddle = false;
+    d.tw_scale = 1;
+    d.tw_line_mul_m = 0;
+    return d;
+  };
+  if (P == 1) {
+    // lines are whole transforms
+    PassDesc d = base(shape.split[0]);
+    d.L_lo = (uint32_t)batch;
+    d.L_b = 1;
+    d.is_lo = d.os_lo = N;
+    d.es_in = d.es_out = 1;
+    d.in_buf = 0;
+    d.out_buf = 2;
+    ps.push_back(d);
+    return ps;
+  }
+  const uint64_t N1 = 1ull << shape.split[0];
+  if (P == 2) {
+    const uint64_t N2 = N / N1;
+    PassDesc a = base(shape.split[0]);  // columns of length N1, stride N2
+    a.L_lo = (uint32_t)N2;
+    a.is_lo = a.os_lo = 1;
+    a.es_in = a.es_out = N2;
+    a.twiddle = true;  // omega_N^(n2 * k1)
+    a.in_buf = 0;
+    a.out_buf = 1;
+    PassDesc b = base(shape.split[1]);  // rows k1 of length N2 -> X[k1 + N1 k2]
+    b.L_lo = (uint32_t)N1;
+    b.is_lo = N2;
+    b.es_in = 1;
+    b.os_lo = 1;
+    b.es_out = N1;
+    b.in_buf = 1;
+    b.out_buf = 2;
+    ps.push_back(a);
+    ps.push_back(b);
+    return ps;
+  }
+  // P == 3: N = N1 * N2 * N3
+  const uint64_t N2 = 1ull << shape.split[1];
+  const uint64_t N3 = 1ull << shape.split[2];
+  const uint64_t M2 = N2 * N3;
+  PassDesc a = base(shape.split[0]);
+  a.L_lo = (uint32_t)M2;
+  a.is_lo = a.os_lo = 1;
+  a.es_in = a.es_out = M2;
+  a.twiddle = true;  // omega_N^(n' * k1)
+  a.in_buf = 0;
+  a.out_buf = 1;
+  PassDesc b = base(shape.split[1]);
+  b.L_lo = (uint32_t)N3;
+  b.L_m = (uint32_t)N1;  // rows k1
+  b.is_lo = b.os_lo = 1;
+  b.is_m = b.os_m = M2;
+  b.es_in = b.es_out = N3;
+  b.twiddle = true;  // omega_{M2}^(n3 * k2) = omega_N^(N1 * n3 * k2)
+  b.tw_scale = N1;
+  b.in_buf = 1;
+  b.out_buf = 1;
+  PassDesc c = base(shape.split[2]);
+  c.L_lo = (uint32_t)N1;  // k1
+  c.L_m = (uint32_t)N2;   // k2
+  c.is_lo = M2;
+  c.is_m = N3;
+  c.es_in = 1;
+  c.os_lo = 1;
+  c.os_m = N1;
+  c.es_out = N1 * N2;
+  c.in_buf = 1;
+  c.out_buf = 2;
+  ps.push_back(a);
+  ps.push_back(b);
+  ps.push_back(c);
+  return ps;
+}
+
+int default_plan(int field, uint32_t log_n, uint64_t batch) {
+  (void)field;
+  (void)log_n;
+  (void)batch;
+  return 0;
+}
+
+static std::string plan_name(const PlanShape& s) {
+  if (s.split.empty()) return "identity";
+  std::string n = s.split.size() == 1 ? "stockham-tile " : "four-step ";
+  for (size_t i = 0; i < s.split.size(); i++) {
+    if (i) n += "x";
+    n += std::to_string(1 << s.split[i]);
+  }
+  return n;
+}
+
+// ------------------------------------------------------------------ domain tables
+template <class F>
+static int build_domain_tables(omr_ntt_domain_s* d) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  const uint64_t p = F::p64();
+  const uint64_t n = d->n;
+  const size_t nlo = (size_t)std::min<uint64_t>(n, 1ull << kTwLoBits);
+  const size_t nhi = (size_t)std::max<uint64_t>(1, n >> kTwLoBits);
+  for (int dir = 0; dir < 2; dir++) {
+    const uint64_t w = dir == 0 ? d->omega : d->omega_inv;
+    std::vector<E> lo(nlo);
+    std::vector<Tw> hi(nhi);
+    uint64_t a = 1;
+    for (size_t i = 0; i < nlo; i++) {
+      if constexpr (F::ID == GOLDILOCKS) {
+        lo[i] = (E)a;
+      } else {
+        lo[i] = F::to_mont_host(a);
+      }
+      a = hmulmod(a, w, p);
+    }
+    const uint64_t step = hpowmod(w, 1ull << kTwLoBits, p);
+    uint64_t b = 1;
+    for (size_t i = 0; i < nhi; i++) {
+      hi[i] = F::make_tw(b);
+      b = hmulmod(b, step, p);
+    }
+    void *dlo = nullptr, *dhi = nullptr;
+    OMR_CUDA_TRY(cudaMalloc(&dlo, sizeof(E) * nlo));
+    OMR_CUDA_TRY(cudaMalloc(&dhi, sizeof(Tw) * nhi));
+    OMR_CUDA_TRY(cudaMemcpy(dlo, lo.data(), sizeof(E) * nlo, cudaMemcpyHostToDevice));
+    OMR_CUDA_TRY(cudaMemcpy(dhi, hi.data(), sizeof(Tw) * nhi, cudaMemcpyHostToDevice));
+    if (dir == 0) {
+      d->tw_lo_f = dlo;
+      d->tw_hi_f = dhi;
+    } else {
+      d->tw_lo_i = dlo;
+      d->tw_hi_i = dhi;
+    }
+  }
+  return OMR_NTT_OK;
+}
+
+int domain_scratch(omr_ntt_domain_s* d, void* stream, size_t bytes, void** out, int slot) {
+  std::lock_guard<std::mutex> lk(d->mu);
+  Scratch& s = d->scratch[std::make_pair(stream, slot)];
+  if (s.bytes < bytes) {
+    if (s.ptr) {
+      // the previous buffer may still be in use by work queued on this stream
+      OMR_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+      OMR_CUDA_TRY(cudaFree(s.ptr));
+      s.ptr = nullptr;
+      s.bytes = 0;
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess)
+      return fail(OMR_NTT_ERR_ALLOC, std::string("scratch cudaMalloc: ") + cudaGetErrorString(e));
+    s.ptr = p;
+    s.bytes = bytes;
+  }
+  *out = s.ptr;
+  return OMR_NTT_OK;
+}
+
+int sub_domain(omr_ntt_domain_s* d, uint32_t log_m, omr_ntt_domain_s** out) {
+  if (log_m == d->log_n) {
+    *out = d;
+    return OMR_NTT_OK;
+  }
+  std::lock_guard<std::mutex> lk(d->mu);
+  auto it = d->subs.find(log_m);
+  if (it != d->subs.end()) {
+    *out = it->second;
+    return OMR_NTT_OK;
+  }
+  omr_ntt_domain_s* s = nullptr;
+  int rc = omr_ntt_domain_create(d->field, log_m, &s);
+  if (rc) return rc;
+  d->subs[log_m] = s;
+  *out = s;
+  return OMR_NTT_OK;
+}
+
+int run_transform(omr_ntt_domain_s* d, int plan, bool inverse, const void* in, void* out,
+                  uint64_t batch, cudaStream_t stream) {
+  if (plan < 0) plan = default_plan(d->field, d->log_n, batch);
+  if (plan >= (int)d->plans.size()) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "plan id out of range");
+  const size_t bytes = (size_t)d->n * batch * word_bytes(d->field);
+  if (d->log_n == 0) {
+    if (in != out) OMR_CUDA_TRY(cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, stream));
+    return OMR_NTT_OK;
+  }
+  std::vector<PassDesc> ps = build_passes(d->log_n, batch, d->plans[plan]);
+  void* scratch = nullptr;
+  if (ps.size() > 1) {
+    int rc = domain_scratch(d, stream, bytes, &scratch);
+    if (rc) return rc;
+  }
+  for (size_t i = 0; i < ps.size(); i++) {
+    const PassDesc& p = ps[i];
+    const void* src = p.in_buf == 0 ? in : (p.in_buf == 1 ? scratch : out);
+    void* dst = p.out_buf == 1 ? scratch : out;
+    bool last = i + 1 == ps.size();
+    int rc = with_field(d->field, [&](auto f) {
+      return launch_pass<decltype(f)>(d, p, inverse, src, dst, last, stream);
+    });
+    if (rc) return rc;
+  }
+  return OMR_NTT_OK;
+}
+
+}  // namespace omr
+
+using namespace omr;
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* omr_ntt_last_error(void) { return g_last_error.c_str(); }
+
+const char* omr_ntt_version(void) { return "omr-ntt-gb300 0.1 (sm_103a)"; }
+
+int omr_ntt_domain_create(int field, uint32_t log_n, omr_ntt_domain_t* out) {
+  if (!out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  if (!valid_field(field)) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown field id");
+  // NttDomain::new asserts log2 N <= TWO_ADICITY (src/encoder.rs:47-51)
+  if ((int)log_n > two_adicity(field))
+    return fail(OMR_NTT_ERR_SIZE, "N=2^" + std::to_string(log_n) +
+                                      " requires log2(N) <= TWO_ADICITY=" +
+                                      std::to_string(two_adicity(field)));
+  if (log_n > 36) return fail(OMR_NTT_ERR_SIZE, "log2(N) > 36 is not supported");
+  auto* d = new (std::nothrow) omr_ntt_domain_s();
+  if (!d) return fail(OMR_NTT_ERR_ALLOC, "domain allocation failed");
+  d->field = field;
+  d->log_n = log_n;
+  d->n = 1ull << log_n;
+  const uint64_t p = modulus(field);
+  d->omega = hpowmod(generator(field), (p - 1) >> log_n, p);
+  d->omega_inv = hpowmod(d->omega, p - 2, p);
+  d->n_inv = hpowmod(d->n % p, p - 2, p);
+  cudaError_t e = cudaGetDevice(&d->device);
+  if (e != cudaSuccess) {
+    delete d;
+    return fail(OMR_NTT_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  }
+  d->plans = enumerate_plans(log_n);
+  int rc = with_field(field, [&](auto f) { return build_domain_tables<decltype(f)>(d); });
+  if (rc == OMR_NTT_OK) {
+    RootTables rt;
+    rc = get_root_tables(field, &rt);
+  }
+  if (rc) {
+    omr_ntt_domain_destroy(d);
+    return rc;
+  }
+  *out = d;
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_domain_destroy(omr_ntt_domain_t d) {
+  if (!d) return OMR_NTT_OK;
+  DeviceGuard g(d->device);
+  cudaDeviceSynchronize();
+  cudaFree(d->tw_lo_f);
+  cudaFree(d->tw_hi_f);
+  cudaFree(d->tw_lo_i);
+  cudaFree(d->tw_hi_i);
+  for (auto& kv : d->scratch) cudaFree(kv.second.ptr);
+  for (auto& kv : d->subs) omr_ntt_domain_destroy(kv.second);
+  delete d;
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_domain_info(omr_ntt_domain_t d, int* field, uint64_t* n, uint32_t* log_n,
+                        uint64_t* omega) {
+  if (!d) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null domain");
+  if (field) *field = d->field;
+  if (n) *n = d->n;
+  if (log_n) *log_n = d->log_n;
+  if (omega) *omega = d->omega;
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_domain_twiddles(omr_ntt_domain_t d, int bitrev, void* out) {
+  if (!d || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  const uint64_t p = modulus(d->field);
+  const uint64_t n = d->n;
+  std::vector<uint64_t> tw(n);
+  uint64_t a = 1;
+  for (uint64_t k = 0; k < n; k++) {
+    tw[k] = a;
+    a = hmulmod(a, d->omega, p);
+  }
+  const bool wide = d->field == GOLDILOCKS;
+  auto put = [&](uint64_t i, uint64_t v) {
+    if (wide)
+      static_cast<uint64_t*>(out)[i] = v;
+    else
+      static_cast<uint32_t*>(out)[i] = (uint32_t)v;
+  };
+  if (!bitrev) {
+    for (uint64_t k = 0; k < n; k++) put(k, tw[k]);
+  } else {
+    const uint32_t lh = d->log_n ? d->log_n - 1 : 0;
+    for (uint64_t i = 0; i < n / 2; i++) {
+      uint64_t r = 0;
+      for (uint32_t b = 0; b < lh; b++) r |= ((i >> b) & 1ull) << (lh - 1 - b);
+      put(i, tw[r]);
+    }
+  }
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_forward(omr_ntt_domain_t d, int plan, const void* in, void* out, uint64_t batch,
+                    void* stream) {
+  if (!d || !in || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  if (batch == 0) return OMR_NTT_OK;
+  DeviceGuard g(d->device);
+  return run_transform(d, plan, false, in, out, batch, (cudaStream_t)stream);
+}
+
+int omr_ntt_inverse(omr_ntt_domain_t d, int plan, const void* in, void* out, uint64_t batch,
+                    void* stream) {
+  if (!d || !in || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  if (batch == 0) return OMR_NTT_OK;
+  DeviceGuard g(d->device);
+  return run_transform(d, plan, true, in, out, batch, (cudaStream_t)stream);
+}
+
+static int host_roundtrip(omr_ntt_domain_t d, int plan, bool inverse, void* host_buf,
+                          uint64_t batch) {
+  if (!d || !host_buf) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  if (batch == 0) return OMR_NTT_OK;
+  DeviceGuard g(d->device);
+  std::lock_guard<std::mutex> lk(d->host_mu);
+  const size_t bytes = (size_t)d->n * batch * word_bytes(d->field);
+  void* dbuf = nullptr;
+  cudaStream_t s = nullptr;
+  int rc = domain_scratch(d, s, bytes, &dbuf, 2);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(dbuf, host_buf, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = fail(OMR_NTT_ERR_CUDA, "host-to-device copy failed");
+  if (!rc) rc = run_transform(d, plan, inverse, dbuf, dbuf, batch, s);
+  if (!rc && cudaMemcpyAsync(host_buf, dbuf, bytes, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    rc = fail(OMR_NTT_ERR_CUDA, "device-to-host copy failed");
+  cudaError_t se = cudaStreamSynchronize(s);
+  if (!rc && se != cudaSuccess) rc = fail(OMR_NTT_ERR_CUDA, cudaGetErrorString(se));
+  return rc;
+}
+
+int omr_ntt_forward_host(omr_ntt_domain_t d, int plan, void* host_buf, uint64_t batch) {
+  return host_roundtrip(d, plan, false, host_buf, batch);
+}
+
+int omr_ntt_inverse_host(omr_ntt_domain_t d, int plan, void* host_buf, uint64_t batch) {
+  return host_roundtrip(d, plan, true, host_buf, batch);
+}
+
+int omr_ntt_plan_count(int field, uint32_t log_n) {
+  if (!valid_field(field)) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown field id");
+  if ((int)log_n > two_adicity(field)) return fail(OMR_NTT_ERR_SIZE, "log2(N) > TWO_ADICITY");
+  return (int)enumerate_plans(log_n).size();
+}
+
+int omr_ntt_plan_describe(int field, uint32_t log_n, int plan, char* buf, size_t cap) {
+  int cnt = omr_ntt_plan_count(field, log_n);
+  if (cnt < 0) return cnt;
+  if (plan < 0) plan = default_plan(field, log_n, 1);
+  if (plan >= cnt) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "plan id out of range");
+  std::string n = plan_name(enumerate_plans(log_n)[plan]);
+  if (buf && cap) {
+    std::strncpy(buf, n.c_str(), cap - 1);
+    buf[cap - 1] = 0;
+  }
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_plan_passes(int field, uint32_t log_n, int plan, uint64_t batch, uint64_t* rec,
+                        int cap) {
+  int cnt = omr_ntt_plan_count(field, log_n);
+  if (cnt < 0) return cnt;
+  if (plan < 0) plan = default_plan(field, log_n, batch);
+  if (plan >= cnt) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "plan id out of range");
+  std::vector<PassDesc> ps =
+      log_n ? build_passes(log_n, batch, enumerate_plans(log_n)[plan]) : std::vector<PassDesc>{};
+  for (int i = 0; i < (int)ps.size() && i < cap && rec; i++) {
+    const PassDesc& p = ps[i];
+    uint64_t* r = rec + 16 * i;
+    r[0] = p.logT;
+    r[1] = p.L_lo;
+    r[2] = p.L_m;
+    r[3] = p.L_b;
+    r[4] = p.is_lo;
+    r[5] = p.is_m;
+    r[6] = p.is_b;
+    r[7] = p.os_lo;
+    r[8] = p.os_m;
+    r[9] = p.os_b;
+    r[10] = p.es_in;
+    r[11] = p.es_out;
+    r[12] = p.twiddle ? 1 : 0;
+    r[13] = p.tw_scale;
+    r[14] = p.tw_line_mul_m;
+    r[15] = (uint64_t)p.in_buf | ((uint64_t)p.out_buf << 8);
+  }
+  return (int)ps.size();
+}
+
+int omr_ntt_plan_run_pass(omr_ntt_domain_t d, int plan, int pass, int inverse, const void* src,
+                          void* scratch, void* dst, uint64_t batch, void* stream) {
+  if (!d || !src || !dst) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  if (plan < 0) plan = default_plan(d->field, d->log_n, batch);
+  if (plan >= (int)d->plans.size()) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "plan id out of range");
+  if (batch == 0 || d->log_n == 0) return OMR_NTT_OK;
+  std::vector<PassDesc> ps = build_passes(d->log_n, batch, d->plans[plan]);
+  if (pass < 0 || pass >= (int)ps.size()) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "pass out of range");
+  const PassDesc& p = ps[pass];
+  if ((p.in_buf == 1 || p.out_buf == 1) && !scratch)
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "this pass needs a scratch buffer");
+  DeviceGuard g(d->device);
+  const void* in = p.in_buf == 0 ? src : (p.in_buf == 1 ? scratch : dst);
+  void* out = p.out_buf == 1 ? scratch : dst;
+  bool last = pass + 1 == (int)ps.size();
+  return with_field(d->field, [&](auto f) {
+    return launch_pass<decltype(f)>(d, p, inverse != 0, in, out, last, (cudaStream_t)stream);
+  });
+}
+
+}  // extern "C"

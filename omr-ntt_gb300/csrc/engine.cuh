@@ -1,0 +1,134 @@
+// engine.cuh -- host-side engine internals shared by the translation units:
+// domain objects, device tables, pass plans and launch helpers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/omr_ntt.h"
+#include "fields.cuh"
+#include "ntt_pass.cuh"
+
+namespace omr {
+
+// ------------------------------------------------------------------ errors
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+#define OMR_CUDA_TRY(expr)                                                        \
+  do {                                                                            \
+    cudaError_t err__ = (expr);                                                   \
+    if (err__ != cudaSuccess)                                                     \
+      return ::omr::fail(OMR_NTT_ERR_CUDA, std::string(#expr) + ": " +          \
+                                               cudaGetErrorString(err__));       \
+  } while (0)
+
+inline int word_bytes(int field) { return field == GOLDILOCKS ? 8 : 4; }
+int two_adicity(int field);
+uint64_t modulus(int field);
+bool valid_field(int field);
+
+// ------------------------------------------------------------------ plans
+// One pass of a plan (see ntt_pass.cuh for the meaning of the fields).
+struct PassDesc {
+  int logT;
+  uint32_t L_lo, L_m;
+  uint64_t L_b;
+  uint64_t is_lo, is_m, is_b, os_lo, os_m, os_b, es_in, es_out;
+  bool twiddle;
+  uint64_t tw_scale;
+  uint32_t tw_line_mul_m;
+  int in_buf, out_buf;  // 0 source, 1 scratch, 2 destination
+};
+
+// A plan = a split of log N into pass sizes (each 1..12, at most 3 passes).
+struct PlanShape {
+  std::vector<int> split;  // log2 of each pass's line length, first pass first
+};
+
+std::vector<PlanShape> enumerate_plans(uint32_t log_n);
+std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanShape& shape);
+int default_plan(int field, uint32_t log_n, uint64_t batch);
+
+// ------------------------------------------------------------------ device tables
+// Per-field in-line roots omega_4096^k, k < 4096 (forward and inverse),
+// stored as F::Tw, built once per device.
+struct RootTables {
+  const void* fwd = nullptr;
+  const void* inv = nullptr;
+};
+int get_root_tables(int field, RootTables* out);
+
+struct Scratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace omr
+
+// The opaque domain object behind omr_ntt_domain_t.
+struct omr_ntt_domain_s {
+  int field;
+  uint32_t log_n;
+  uint64_t n;
+  uint64_t omega, omega_inv, n_inv;
+  int device;
+  // four-step twiddle tables (device): lo = omega^i (i < 4096, twiddle-Montgomery form),
+  // hi = omega^(4096 i) as F::Tw; forward and inverse
+  void* tw_lo_f = nullptr;
+  void* tw_hi_f = nullptr;
+  void* tw_lo_i = nullptr;
+  void* tw_hi_i = nullptr;
+  std::mutex mu;       // guards `scratch`
+  std::mutex host_mu;  // serialises the synchronous host-buffer calls
+  std::map<std::pair<void*, int>, omr::Scratch> scratch;  // keyed by (stream, slot)
+  std::vector<omr::PlanShape> plans;
+  std::map<uint32_t, omr_ntt_domain_s*> subs;  // smaller domains (same field) for partial paths
+};
+
+namespace omr {
+// Scratch of at least `bytes` for (`stream`, `slot`) (grows; owned by the domain).
+// Slot 0 is the transform passes' intermediate, slot 1 the partial-output
+// staging, slot 2 host-call staging.
+int domain_scratch(omr_ntt_domain_s* d, void* stream, size_t bytes, void** out, int slot = 0);
+
+// The domain of size 2^log_m (same field), created on first use and owned by d.
+int sub_domain(omr_ntt_domain_s* d, uint32_t log_m, omr_ntt_domain_s** out);
+
+// Run one full forward/inverse transform plan (device pointers).
+int run_transform(omr_ntt_domain_s* d, int plan, bool inverse, const void* in, void* out,
+                  uint64_t batch, cudaStream_t stream);
+
+// Field dispatch: calls fn(F{}) for the field's type.
+template <class Fn>
+int with_field(int field, Fn&& fn) {
+  switch (field) {
+    case BABYBEAR: return fn(BabyBear{});
+    case GOLDILOCKS: return fn(Goldilocks{});
+    case KOALABEAR: return fn(KoalaBear{});
+    case TEDDYBEAR: return fn(TeddyBear{});
+  }
+  return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown field id");
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Typed launch of one pass.
+template <class F>
+int launch_pass(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, const void* in,
+                void* out, bool last, cudaStream_t stream);
+}  // namespace omr

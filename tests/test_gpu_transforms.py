@@ -1,0 +1,118 @@
+"""GPU parity: forward / inverse NTTs through the C ABI against the oracle,
+bit-exact, every field, every plan, sizes 2^0 .. 2^24 and batches."""
+import numpy as np
+import pytest
+
+import omr_ntt
+from omr_ntt import NttDomain, OmrNttError
+from omr_ntt.fields import ALL, BabyBear, Goldilocks, KoalaBear, TeddyBear
+from omr_ntt.inputs import gen_input_seeded
+from gpu_util import to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("field", ALL, ids=lambda f: f.name)
+def test_forward_all_plans_small(oracle, field):
+    for log_n in range(0, 15):
+        n = 1 << log_n
+        d = NttDomain(field, n)
+        x = gen_input_seeded(field, n, 31 + log_n)
+        exp = oracle.forward(field.id, x)
+        for plan in range(omr_ntt.plan_count(field, log_n)):
+            got = omr_ntt.forward(d, x, plan=plan)
+            assert np.array_equal(got, exp), (field, log_n, plan)
+            back = omr_ntt.inverse(d, got, plan=plan)
+            assert np.array_equal(back, x), (field, log_n, plan)
+
+
+@pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
+@pytest.mark.parametrize("log_n", [16, 18, 20, 22, 24])
+def test_forward_inverse_large(oracle, field, log_n):
+    n = 1 << log_n
+    d = NttDomain(field, n)
+    x = gen_input_seeded(field, n, 42)
+    exp = oracle.forward(field.id, x)
+    xd = to_dev(x)
+    for plan in range(omr_ntt.plan_count(field, log_n)):
+        yd = xd.clone()
+        omr_ntt.forward(d, yd, plan=plan)
+        assert np.array_equal(to_host(yd, field.dtype), exp), plan
+        omr_ntt.inverse(d, yd, plan=plan)
+        assert np.array_equal(to_host(yd, field.dtype), x), plan
+
+
+@pytest.mark.parametrize("field", [KoalaBear, TeddyBear], ids=lambda f: f.name)
+def test_other_fields_large(oracle, field):
+    for log_n in (17, 21):
+        n = 1 << log_n
+        d = NttDomain(field, n)
+        x = gen_input_seeded(field, n, 3)
+        got = omr_ntt.forward(d, x)
+        assert np.array_equal(got, oracle.forward(field.id, x))
+        assert np.array_equal(omr_ntt.inverse(d, got), x)
+
+
+@pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
+def test_batch_64_of_2_20(oracle, field):
+    log_n, batch = 20, 64
+    n = 1 << log_n
+    d = NttDomain(field, n)
+    x = gen_input_seeded(field, n * batch, 77)
+    xd = to_dev(x)
+    yd = xd.clone()
+    omr_ntt.forward(d, yd, batch=batch)
+    y = to_host(yd, field.dtype)
+    for b in (0, 1, 37, 63):
+        seg = slice(b * n, (b + 1) * n)
+        assert np.array_equal(y[seg], oracle.forward(field.id, x[seg])), b
+    omr_ntt.inverse(d, yd, batch=batch)
+    assert np.array_equal(to_host(yd, field.dtype), x)
+
+
+@pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
+def test_out_of_place_and_in_place_agree(oracle, field):
+    n = 1 << 14
+    d = NttDomain(field, n)
+    x = gen_input_seeded(field, n, 5)
+    xd = to_dev(x)
+    out = xd.clone().zero_()
+    omr_ntt.forward(d, xd, out=out)
+    assert np.array_equal(to_host(xd, field.dtype), x)  # input untouched
+    assert np.array_equal(to_host(out, field.dtype), oracle.forward(field.id, x))
+
+
+def test_log_n_27_babybear(oracle):
+    # the reference's own bench size (benches/ntt_bench_n.rs:7): 2^27, three passes
+    n = 1 << 27
+    d = NttDomain(BabyBear, n)
+    x = gen_input_seeded(BabyBear, n, 42)
+    xd = to_dev(x)
+    omr_ntt.forward(d, xd)
+    y = to_host(xd, BabyBear.dtype)
+    oracle.set_threads(0)
+    assert np.array_equal(y, oracle.forward(BabyBear.id, x))
+
+
+def test_size_errors():
+    with pytest.raises(OmrNttError):
+        NttDomain(BabyBear, 1 << 28)
+    with pytest.raises(OmrNttError):
+        NttDomain(BabyBear, 12)
+    with pytest.raises(OmrNttError):
+        NttDomain(KoalaBear, 1 << 25)
+
+
+def test_noncanonical_check():
+    n = 1 << 12
+    d = NttDomain(BabyBear, n)
+    x = gen_input_seeded(BabyBear, n, 1)
+    from omr_ntt import _lib
+    import ctypes
+
+    xd = to_dev(x)
+    assert _lib.lib().omr_ntt_check_canonical(d.handle, ctypes.c_void_p(xd.data_ptr()), n, None) == 0
+    x2 = x.copy()
+    x2[100] = BabyBear.p
+    xd2 = to_dev(x2)
+    assert _lib.lib().omr_ntt_check_canonical(d.handle, ctypes.c_void_p(xd2.data_ptr()), n, None) == -7
