@@ -99,6 +99,11 @@ int omr_ntt_domain_create(int field, uint32_t log_n, omr_ntt_domain_t *out);
 /* Drop of NttDomain: frees device tables and every per-stream scratch buffer. */
 int omr_ntt_domain_destroy(omr_ntt_domain_t d);
 
+/* Synchronise `stream` and report whether any kernel of this domain hit a
+ * bounded device-side wait limit since the last check (OMR_NTT_ERR_TIMEOUT;
+ * the word is then cleared).  Host-buffer calls check it themselves. */
+int omr_ntt_domain_check(omr_ntt_domain_t d, void *stream);
+
 /* NttDomain fields N, log_N, omega (src/encoder.rs:30-33); omega canonical. */
 int omr_ntt_domain_info(omr_ntt_domain_t d, int *field, uint64_t *n, uint32_t *log_n,
                         uint64_t *omega);

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "launch_pass.cuh"
 
 namespace omr {
 
@@ -102,24 +103,58 @@ int get_root_tables(int field, RootTables* out) {
   return OMR_NTT_OK;
 }
 
+// ------------------------------------------------------------------ driver helpers
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::atomic<PFN_cuTensorMapEncodeTiled_v12000> fn{nullptr};
+  PFN_cuTensorMapEncodeTiled_v12000 f = fn.load();
+  if (!f) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess) {
+      f = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+      fn.store(f);
+    }
+  }
+  return f;
+}
+
+int device_sm_count(int dev) {
+  static std::atomic<int> cache[64];
+  int v = cache[dev & 63].load();
+  if (v <= 0) {
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    if (v <= 0) v = 1;
+    cache[dev & 63] = v;
+  }
+  return v;
+}
+
 // ------------------------------------------------------------------ plans
 std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
   std::vector<PlanShape> out;
   if (log_n == 0) {
-    out.push_back(PlanShape{{}});
+    out.push_back(PlanShape{{}, 0});
     return out;
   }
   int pmin = (int)((log_n + kMaxLogT - 1) / kMaxLogT);
   if (pmin < 1) pmin = 1;
+  std::vector<std::vector<int>> splits;
   for (int P = pmin; P <= std::min(3, pmin + 1); P++) {
     if ((uint32_t)P > log_n) break;
     std::vector<int> s(P);
     for (int i = 0; i < P; i++) s[i] = (int)(log_n / P) + (i < (int)(log_n % P) ? 1 : 0);
     if (s[0] > kMaxLogT) continue;
-    out.push_back(PlanShape{s});
+    splits.push_back(s);
     std::vector<int> r(s.rbegin(), s.rend());
-    if (r != s) out.push_back(PlanShape{r});
+    if (r != s) splits.push_back(r);
   }
+  for (int v = 0; v < 3; v++)
+    for (auto& s : splits) {
+      if (v > 0 && s.size() == 1) continue;  // single-pass plans have one kernel
+      out.push_back(PlanShape{s, v});
+    }
   return out;
 }
 
@@ -148,6 +183,8 @@ std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanSha
     d.es_in = d.es_out = 1;
     d.in_buf = 0;
     d.out_buf = 2;
+    d.mode = MODE_LINE;
+    d.variant = 0;
     ps.push_back(d);
     return ps;
   }
@@ -169,6 +206,9 @@ std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanSha
     b.es_out = N1;
     b.in_buf = 1;
     b.out_buf = 2;
+    a.mode = MODE_COL;
+    b.mode = MODE_ROW;
+    a.variant = b.variant = shape.variant;
     ps.push_back(a);
     ps.push_back(b);
     return ps;
@@ -205,6 +245,9 @@ std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanSha
   c.es_out = N1 * N2;
   c.in_buf = 1;
   c.out_buf = 2;
+  a.mode = b.mode = MODE_COL;
+  c.mode = MODE_ROW;
+  a.variant = b.variant = c.variant = shape.variant;
   ps.push_back(a);
   ps.push_back(b);
   ps.push_back(c);
@@ -225,6 +268,7 @@ static std::string plan_name(const PlanShape& s) {
     if (i) n += "x";
     n += std::to_string(1 << s.split[i]);
   }
+  if (s.split.size() > 1) n += s.variant == 0 ? " tile" : (s.variant == 1 ? " tma" : " tma-wide");
   return n;
 }
 
@@ -377,6 +421,10 @@ int omr_ntt_domain_create(int field, uint32_t log_n, omr_ntt_domain_t* out) {
     return fail(OMR_NTT_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   }
   d->plans = enumerate_plans(log_n);
+  if (cudaMalloc(&d->err, sizeof(int)) != cudaSuccess || cudaMemset(d->err, 0, sizeof(int)) != cudaSuccess) {
+    omr_ntt_domain_destroy(d);
+    return fail(OMR_NTT_ERR_ALLOC, "error-word allocation failed");
+  }
   int rc = with_field(field, [&](auto f) { return build_domain_tables<decltype(f)>(d); });
   if (rc == OMR_NTT_OK) {
     RootTables rt;
@@ -394,6 +442,7 @@ int omr_ntt_domain_destroy(omr_ntt_domain_t d) {
   if (!d) return OMR_NTT_OK;
   DeviceGuard g(d->device);
   cudaDeviceSynchronize();
+  cudaFree(d->err);
   cudaFree(d->tw_lo_f);
   cudaFree(d->tw_hi_f);
   cudaFree(d->tw_lo_i);
@@ -401,6 +450,20 @@ int omr_ntt_domain_destroy(omr_ntt_domain_t d) {
   for (auto& kv : d->scratch) cudaFree(kv.second.ptr);
   for (auto& kv : d->subs) omr_ntt_domain_destroy(kv.second);
   delete d;
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_domain_check(omr_ntt_domain_t d, void* stream) {
+  if (!d) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null domain");
+  DeviceGuard g(d->device);
+  int h = 0;
+  OMR_CUDA_TRY(cudaMemcpyAsync(&h, d->err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  OMR_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  if (h) {
+    OMR_CUDA_TRY(cudaMemsetAsync(d->err, 0, sizeof(int), (cudaStream_t)stream));
+    OMR_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return fail(h, "a device-side bounded wait gave up (the affected outputs are invalid)");
+  }
   return OMR_NTT_OK;
 }
 
@@ -478,6 +541,7 @@ static int host_roundtrip(omr_ntt_domain_t d, int plan, bool inverse, void* host
     rc = fail(OMR_NTT_ERR_CUDA, "device-to-host copy failed");
   cudaError_t se = cudaStreamSynchronize(s);
   if (!rc && se != cudaSuccess) rc = fail(OMR_NTT_ERR_CUDA, cudaGetErrorString(se));
+  if (!rc) rc = omr_ntt_domain_check(d, s);
   return rc;
 }
 

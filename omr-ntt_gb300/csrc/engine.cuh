@@ -42,11 +42,14 @@ struct PassDesc {
   uint64_t tw_scale;
   uint32_t tw_line_mul_m;
   int in_buf, out_buf;  // 0 source, 1 scratch, 2 destination
+  int mode;             // PassMode (ntt_pass.cuh)
+  int variant;          // 0: ntt_tile_pass; 1, 2: ntt_tile_pass_tma (two thread counts)
 };
 
 // A plan = a split of log N into pass sizes (each 1..12, at most 3 passes).
 struct PlanShape {
   std::vector<int> split;  // log2 of each pass's line length, first pass first
+  int variant = 0;         // pass kernel variant of the multi-pass plans
 };
 
 std::vector<PlanShape> enumerate_plans(uint32_t log_n);
@@ -82,6 +85,7 @@ struct omr_ntt_domain_s {
   void* tw_hi_f = nullptr;
   void* tw_lo_i = nullptr;
   void* tw_hi_i = nullptr;
+  int* err = nullptr;  // device error word raised by bounded waits (OMR_NTT_ERR_TIMEOUT)
   std::mutex mu;       // guards `scratch`
   std::mutex host_mu;  // serialises the synchronous host-buffer calls
   std::map<std::pair<void*, int>, omr::Scratch> scratch;  // keyed by (stream, slot)

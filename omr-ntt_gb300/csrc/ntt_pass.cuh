@@ -2,20 +2,25 @@
 //
 // Every full transform in this engine is a sequence of passes.  A pass runs
 // a batch of independent T-point NTTs ("lines", T = 2^LOGT <= 4096).  One CTA
-// owns C adjacent lines (C * word = 32 bytes, one DRAM sector per row of the
-// tile), loads the T x C tile into shared memory with coalesced accesses,
-// runs the T-point transform as radix-2^r Stockham rounds (each round: every
-// thread pulls R = 2^r words per butterfly into registers, applies the
-// round's twiddles, runs an R-point DFT with compile-time roots, and writes
-// the R results back in autosorted order), then stores the tile, optionally
-// multiplying each output by the four-step twiddle omega_N^(line * k * scale)
-// and/or the inverse-transform scale N^-1.
+// owns C adjacent lines and runs their T-point transforms as radix-2^r
+// Stockham rounds: each thread pulls R = 2^r words per butterfly into
+// registers, applies the round's twiddles, runs an R-point DFT with
+// compile-time roots, and writes the R results in autosorted order.
+//
+//   * The first round reads global memory straight into registers when
+//     adjacent lines are adjacent words (column passes): every load of the
+//     thread is issued before the first use, so a CTA keeps T*C/NT loads in
+//     flight.  Row passes (a line is a contiguous run) stage the tile through
+//     shared memory with the same all-loads-first pattern.
+//   * Middle rounds exchange through a swizzled shared-memory tile.
+//   * The last round writes global memory straight from registers, applying
+//     the four-step twiddle omega_N^(line * k * scale) and the inverse scale.
 //
 // The pass is the GB300 counterpart of the reference's sub-NTT building
 // blocks (inplace_radix2_dit / inplace_radix2_dif_no_derange,
 // src/encoders/utils.rs:26-83), its transposes (transpose_par,
 // src/encoders/transpose_out_of_place.rs:340-366; here folded into the
-// strided tile loads/stores) and the four-step twiddle scaling
+// tile loads/stores) and the four-step twiddle scaling
 // (src/encoders/winterfell_four_step.rs:63-78).
 #pragma once
 #include <cstdint>
@@ -24,8 +29,15 @@
 
 namespace omr {
 
-constexpr int kMaxLogT = 12;  // largest line handled by one pass (4096 points)
-constexpr int kTwLoBits = 12; // two-level four-step twiddle split
+constexpr int kMaxLogT = 12;   // largest line handled by one pass (4096 points)
+constexpr int kTwLoBits = 12;  // two-level four-step twiddle split
+
+// Pass modes (how lines sit in memory).
+enum PassMode : int {
+  MODE_COL = 0,   // adjacent lines are adjacent words on both sides (is_lo = os_lo = 1)
+  MODE_ROW = 1,   // a line is a contiguous run on input (es_in = 1), adjacent on output (os_lo = 1)
+  MODE_LINE = 2,  // a line is a contiguous run on both sides (es_in = es_out = 1)
+};
 
 template <class F>
 struct PassArgs {
@@ -35,18 +47,20 @@ struct PassArgs {
   E* out;
   // line geometry: line index = (lb, lm, llo); llo is the fast (adjacent) index
   uint32_t L_lo, L_m;
+  uint64_t L_b;
   uint64_t is_lo, is_m, is_b;  // input strides of the line index components
   uint64_t os_lo, os_m, os_b;  // output strides
-  uint64_t es_in, es_out;      // element strides along a line
+  uint32_t es_in, es_out;      // element strides along a line (within a transform: < 2^31)
   // in-line roots: roots[k * roots_stride] = omega_T^k (forward or inverse)
   const Tw* roots;
   uint32_t roots_stride;
-  // four-step twiddle on outputs: exponent e = (tw_line(llo, lm) * k * tw_scale) mod N
-  const E* tw_lo;   // omega^i (i < 2^12), "twiddle-Montgomery" form; null = no twiddle
+  // four-step twiddle on outputs: exponent e = (tw_line * k * tw_scale) mod N,
+  // tw_line = llo + lm * tw_line_mul_m; tw_lo == nullptr disables it
+  const E* tw_lo;   // omega^i (i < 2^12), "twiddle-Montgomery" form
   const Tw* tw_hi;  // omega^(2^12 i)
-  uint64_t tw_scale;
-  uint64_t tw_mask;  // N - 1
-  uint32_t tw_line_mul_m;  // tw_line = llo + lm * tw_line_mul_m
+  uint32_t tw_scale;
+  uint32_t tw_mask;  // N - 1
+  uint32_t tw_line_mul_m;
   int has_scale;
   Tw scale;  // N^-1 for inverse transforms
 };
@@ -78,18 +92,6 @@ struct RootConst {
   static constexpr typename F::Tw tw = F::make_tw(value);
 };
 
-template <class F, int LOGR, int K, bool INV>
-OMR_D typename F::E mul_root(typename F::E x) {
-  constexpr int R = 1 << LOGR;
-  constexpr int KK = INV ? ((R - K) % R) : K;
-  if constexpr (KK == 0) {
-    return x;
-  } else {
-    constexpr typename F::Tw t = RootConst<F, LOGR, KK>::tw;
-    return F::mul_tw(x, t);
-  }
-}
-
 // In-register R-point DFT (R = 2^LOGR), natural order in and out.
 // Radix-2 decimation in frequency: (u + v, (u - v) * omega_len^j), outputs in
 // bit-reversed register order, undone by compile-time renaming.
@@ -102,7 +104,6 @@ OMR_D void dif_stage_bf(typename F::E* v) {
   if constexpr (J == 0) {
     v[BLK + J + HALF] = F::sub(u, w);
   } else {
-    // omega_len^J with len = 2^LEN_LOG
     constexpr int K = J << (LOGR - LEN_LOG);
     constexpr int R = 1 << LOGR;
     constexpr int KK = INV ? ((R - K) % R) : K;
@@ -150,12 +151,12 @@ OMR_D void dft_reg(typename F::E (&v)[1 << LOGR]) {
 }
 
 // Shared-memory tile [T rows][C cols] with an XOR swizzle so that both a
-// column walk (32 consecutive rows, one column) and a row walk (consecutive
+// column walk (consecutive rows, one column) and a row walk (consecutive
 // columns, a few consecutive rows) are free of bank conflicts.
 template <class F, int C>
 OMR_D int tile_idx(int t, int c) {
-  constexpr int ROWB = C * F::WORD;                  // bytes per tile row
-  constexpr int SW = ROWB >= 128 ? 1 : 128 / ROWB;   // rows per 128-byte bank line
+  constexpr int ROWB = C * F::WORD;                 // bytes per tile row
+  constexpr int SW = ROWB >= 128 ? 1 : 128 / ROWB;  // rows per 128-byte bank line
   return t * C + (c ^ ((t / SW) & (C - 1)));
 }
 
@@ -171,134 +172,171 @@ struct RoundPlan {
   }
 };
 
-// One Stockham round in shared memory (in place: all reads, barrier, writes).
-template <class F, int LOGT, int C, int NT, int LOGR, int LOGNS, bool INV>
-OMR_D void stockham_round(typename F::E* s, const typename F::Tw* __restrict__ roots,
-                          uint32_t roots_stride) {
-  using E = typename F::E;
-  constexpr int T = 1 << LOGT, R = 1 << LOGR, NS = 1 << LOGNS;
-  constexpr int NB = (T / R) * C;
-  constexpr int PER = (NB + NT - 1) / NT;
-  E v[PER][R];
-#pragma unroll
-  for (int i = 0; i < PER; i++) {
-    int b = threadIdx.x + i * NT;
-    if (NB % NT == 0 || b < NB) {
-      int c = b % C, j = b / C;
-#pragma unroll
-      for (int q = 0; q < R; q++) v[i][q] = s[tile_idx<F, C>(j + q * (T / R), c)];
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int i = 0; i < PER; i++) {
-    int b = threadIdx.x + i * NT;
-    if (NB % NT == 0 || b < NB) {
-      int c = b % C, j = b / C;
-      int jm = j & (NS - 1);
-      if constexpr (LOGNS > 0) {
-        // a_q *= omega_{NS*R}^{q*jm} = omega_T^{q*jm*T/(NS*R)}
-        constexpr int SCALE = T / (NS * R);
-#pragma unroll
-        for (int q = 1; q < R; q++)
-          v[i][q] = F::mul_tw(v[i][q], roots[(uint32_t)(q * jm * SCALE) * roots_stride]);
-      }
-      dft_reg<F, LOGR, INV>(v[i]);
-      int d = ((j >> LOGNS) << (LOGNS + LOGR)) | jm;
-#pragma unroll
-      for (int q = 0; q < R; q++) s[tile_idx<F, C>(d + q * NS, c)] = v[i][q];
-    }
-  }
-  __syncthreads();
-}
-
-template <class F, int LOGT, int C, int NT, int MAXR, bool INV, int I>
-OMR_D void all_rounds(typename F::E* s, const typename F::Tw* roots, uint32_t roots_stride) {
-  using RP = RoundPlan<LOGT, MAXR>;
-  if constexpr (I < RP::ROUNDS) {
-    stockham_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), INV>(s, roots, roots_stride);
-    all_rounds<F, LOGT, C, NT, MAXR, INV, I + 1>(s, roots, roots_stride);
-  }
-}
-
 template <class F>
 constexpr int max_radix_log() {
   return F::WORD == 8 ? 3 : 4;
 }
 
-template <class F, int LOGT>
-constexpr int pass_threads() {
-  constexpr int C = 32 / F::WORD;
-  constexpr int TC = (1 << LOGT) * C;
-  constexpr int nt = TC / 16;
-  return nt < 32 ? 32 : (nt > 512 ? 512 : nt);
+// Tile variants: V = 0 -> C = 32 bytes of lines (one DRAM sector per tile
+// row), V = 1 -> C = 16 bytes (half the shared memory: two CTAs per SM at
+// 4096-point lines).  Threads give each thread EPT elements.
+template <class F, int V>
+constexpr int tile_cols() {
+  return (V == 0 ? 32 : 16) / F::WORD;
+}
+template <class F>
+constexpr int tile_ept() {
+  return F::WORD == 8 ? 32 : 64;
+}
+template <class F, int LOGT, int V>
+constexpr int tile_threads() {
+  constexpr int TC = (1 << LOGT) * tile_cols<F, V>();
+  constexpr int nt = TC / tile_ept<F>();
+  return nt < 32 ? 32 : (nt > 1024 ? 1024 : nt);
+}
+template <class F, int LOGT, int V>
+constexpr int tile_min_blocks() {
+  // keep <= 128 registers per thread for the 64-element tiles
+  return tile_threads<F, LOGT, V>() >= 512 ? 1 : (65536 / 128) / tile_threads<F, LOGT, V>();
+}
+
+enum { SRC_GLOBAL = 0, SRC_SMEM = 1 };
+enum { DST_SMEM = 0, DST_GLOBAL = 1 };
+
+// One Stockham round.  SRC_GLOBAL reads the column-pass input directly (c-fast
+// mapping: 8 lines x 4 rows per warp, one sector per row); DST_GLOBAL writes
+// the output directly (c-fast, or j-fast for MODE_LINE so a warp writes 32
+// consecutive words of one line).
+template <class F, int LOGT, int C, int NT, int LOGR, int LOGNS, bool INV, int SRC, int DST,
+          bool JF, bool TW>
+OMR_D void do_round(const PassArgs<F>& a, typename F::E* s, const typename F::E* __restrict__ gin,
+                    typename F::E* __restrict__ gout, int nvalid, uint32_t llo0, uint32_t lm) {
+  using E = typename F::E;
+  constexpr int T = 1 << LOGT, R = 1 << LOGR, NS = 1 << LOGNS;
+  constexpr int TR = T / R;
+  constexpr int NB = TR * C;
+  constexpr int PER = (NB + NT - 1) / NT;
+  E v[PER][R];
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int b = threadIdx.x + i * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = JF ? b / TR : b % C;
+      const int j = JF ? b % TR : b / C;
+#pragma unroll
+      for (int q = 0; q < R; q++) {
+        const int t = j + q * TR;
+        if constexpr (SRC == SRC_GLOBAL) {
+          v[i][q] = c < nvalid ? gin[(uint32_t)c + (uint32_t)t * a.es_in] : (E)0;
+        } else {
+          v[i][q] = s[tile_idx<F, C>(t, c)];
+        }
+      }
+    }
+  }
+  if constexpr (SRC == SRC_SMEM && DST == DST_SMEM) __syncthreads();
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int b = threadIdx.x + i * NT;
+    if (NB % NT == 0 || b < NB) {
+      const int c = JF ? b / TR : b % C;
+      const int j = JF ? b % TR : b / C;
+      const int jm = j & (NS - 1);
+      if constexpr (LOGNS > 0) {
+        // a_q *= omega_{NS*R}^{q*jm} = omega_T^{q*jm*T/(NS*R)}
+        constexpr int SCALE = T / (NS * R);
+#pragma unroll
+        for (int q = 1; q < R; q++)
+          v[i][q] = F::mul_tw(v[i][q], a.roots[(uint32_t)(q * jm * SCALE) * a.roots_stride]);
+      }
+      dft_reg<F, LOGR, INV>(v[i]);
+      const int d = ((j >> LOGNS) << (LOGNS + LOGR)) | jm;
+#pragma unroll
+      for (int q = 0; q < R; q++) {
+        const int k = d + q * NS;
+        if constexpr (DST == DST_SMEM) {
+          s[tile_idx<F, C>(k, c)] = v[i][q];
+        } else {
+          if (c < nvalid) {
+            E y = v[i][q];
+            if constexpr (TW) {
+              if (a.tw_lo != nullptr) {
+                const uint32_t line = llo0 + (uint32_t)c + lm * a.tw_line_mul_m;
+                const uint32_t e = (line * (uint32_t)k * a.tw_scale) & a.tw_mask;
+                const E tm = F::mul_tw(a.tw_lo[e & ((1u << kTwLoBits) - 1)], a.tw_hi[e >> kTwLoBits]);
+                y = mul_m<F>(y, tm);
+              }
+            }
+            if (a.has_scale) y = F::mul_tw(y, a.scale);
+            if constexpr (JF)
+              gout[(uint64_t)c * a.os_lo + (uint32_t)k] = y;
+            else
+              gout[(uint32_t)c + (uint32_t)k * a.es_out] = y;
+          }
+        }
+      }
+    }
+  }
+  if constexpr (DST == DST_SMEM) __syncthreads();
+}
+
+template <class F, int LOGT, int C, int NT, int MODE, bool INV, int I>
+OMR_D void all_rounds(const PassArgs<F>& a, typename F::E* s, const typename F::E* gin,
+                      typename F::E* gout, int nvalid, uint32_t llo0, uint32_t lm) {
+  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  if constexpr (I < RP::ROUNDS) {
+    constexpr bool first = I == 0, last = I + 1 == RP::ROUNDS;
+    constexpr int SRC = (first && MODE == MODE_COL) ? SRC_GLOBAL : SRC_SMEM;
+    constexpr int DST = last ? DST_GLOBAL : DST_SMEM;
+    constexpr bool JF = last && MODE == MODE_LINE;
+    constexpr bool TW = MODE == MODE_COL;
+    do_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), INV, SRC, DST, JF, TW>(a, s, gin, gout,
+                                                                              nvalid, llo0, lm);
+    all_rounds<F, LOGT, C, NT, MODE, INV, I + 1>(a, s, gin, gout, nvalid, llo0, lm);
+  }
 }
 
 // ------------------------------------------------------------------ kernel
-template <class F, int LOGT, bool INV>
-__global__ void __launch_bounds__(pass_threads<F, LOGT>())
+template <class F, int LOGT, int V, int MODE, bool INV>
+__global__ void __launch_bounds__(tile_threads<F, LOGT, V>(), tile_min_blocks<F, LOGT, V>())
     ntt_tile_pass(const PassArgs<F> a) {
   using E = typename F::E;
   constexpr int T = 1 << LOGT;
-  constexpr int C = 32 / F::WORD;
-  constexpr int NT = pass_threads<F, LOGT>();
+  constexpr int C = tile_cols<F, V>();
+  constexpr int NT = tile_threads<F, LOGT, V>();
   constexpr int TC = T * C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E* s = reinterpret_cast<E*>(smem_raw);
 
   const uint32_t groups = (a.L_lo + C - 1) / C;
-  uint64_t blk = blockIdx.x;
-  const uint32_t g = (uint32_t)(blk % groups);
+  uint32_t blk = blockIdx.x;
+  const uint32_t g = blk % groups;
   blk /= groups;
-  const uint32_t lm = (uint32_t)(blk % a.L_m);
+  const uint32_t lm = blk % a.L_m;
   const uint64_t lb = blk / a.L_m;
   const uint32_t llo0 = g * C;
-  const uint64_t in_base = lb * a.is_b + lm * a.is_m + llo0 * a.is_lo;
-  const uint64_t out_base = lb * a.os_b + lm * a.os_m + llo0 * a.os_lo;
+  const E* gin = a.in + (lb * a.is_b + lm * a.is_m + llo0 * a.is_lo);
+  E* gout = a.out + (lb * a.os_b + lm * a.os_m + llo0 * a.os_lo);
+  const int nvalid = (int)min((uint32_t)C, a.L_lo - llo0);
 
-  // ---- load tile: c-fastest when adjacent lines are adjacent in memory
-  const bool in_cfast = (a.is_lo == 1);
-  for (int i = threadIdx.x; i < TC; i += NT) {
-    int t, c;
-    if (in_cfast) {
-      c = i % C;
-      t = i / C;
-    } else {
-      t = i % T;
-      c = i / T;
+  if constexpr (MODE != MODE_COL) {
+    // stage the tile: consecutive threads read consecutive words of one line
+    constexpr int PER = (TC + NT - 1) / NT;
+    E r[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const int idx = threadIdx.x + i * NT;
+      const int t = idx % T, c = idx / T;
+      r[i] = (TC % NT == 0 || idx < TC) && c < nvalid ? gin[(uint64_t)c * a.is_lo + (uint32_t)t] : (E)0;
     }
-    E x = 0;
-    if (llo0 + c < a.L_lo) x = a.in[in_base + (uint64_t)c * a.is_lo + (uint64_t)t * a.es_in];
-    s[tile_idx<F, C>(t, c)] = x;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const int idx = threadIdx.x + i * NT;
+      if (TC % NT == 0 || idx < TC) s[tile_idx<F, C>(idx % T, idx / T)] = r[i];
+    }
+    __syncthreads();
   }
-  __syncthreads();
-
-  all_rounds<F, LOGT, C, NT, max_radix_log<F>(), INV, 0>(s, a.roots, a.roots_stride);
-
-  // ---- store tile (+ four-step twiddle, + inverse scale)
-  const bool out_cfast = (a.os_lo == 1);
-  for (int i = threadIdx.x; i < TC; i += NT) {
-    int k, c;
-    if (out_cfast) {
-      c = i % C;
-      k = i / C;
-    } else {
-      k = i % T;
-      c = i / T;
-    }
-    if (llo0 + c >= a.L_lo) continue;
-    E y = s[tile_idx<F, C>(k, c)];
-    if (a.tw_lo != nullptr) {
-      uint64_t line = (uint64_t)(llo0 + c) + (uint64_t)lm * a.tw_line_mul_m;
-      uint64_t e = (line * (uint64_t)k * a.tw_scale) & a.tw_mask;
-      if (e != 0) {
-        E tm = F::mul_tw(a.tw_lo[e & ((1u << kTwLoBits) - 1)], a.tw_hi[e >> kTwLoBits]);
-        y = mul_m<F>(y, tm);
-      }
-    }
-    if (a.has_scale) y = F::mul_tw(y, a.scale);
-    a.out[out_base + (uint64_t)c * a.os_lo + (uint64_t)k * a.es_out] = y;
-  }
+  all_rounds<F, LOGT, C, NT, MODE, INV, 0>(a, s, gin, gout, nvalid, llo0, lm);
 }
 
 }  // namespace omr

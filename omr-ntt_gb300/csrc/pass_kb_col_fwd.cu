@@ -1,0 +1,10 @@
+// pass_kb_col_fwd.cu -- KoalaBear tile passes, MODE_COL, forward
+// (one translation unit per field, mode and direction: parallel compiles).
+#include "launch_pass.cuh"
+
+namespace omr {
+template int launch_pass_dir<KoalaBear, MODE_COL, false>(int, int, const PassArgs<KoalaBear>&, uint64_t, int*,
+                                                     cudaStream_t);
+template int launch_pass<KoalaBear>(const omr_ntt_domain_s*, const PassDesc&, bool, const void*, void*,
+                             bool, cudaStream_t);
+}  // namespace omr

@@ -1,0 +1,8 @@
+// pass_kb_col_inv.cu -- KoalaBear tile passes, MODE_COL, inverse
+// (one translation unit per field, mode and direction: parallel compiles).
+#include "launch_pass.cuh"
+
+namespace omr {
+template int launch_pass_dir<KoalaBear, MODE_COL, true>(int, int, const PassArgs<KoalaBear>&, uint64_t, int*,
+                                                     cudaStream_t);
+}  // namespace omr

@@ -42,6 +42,7 @@ _SIGS = {
     "omr_ntt_domain_destroy": (_c.c_int, [_c.c_void_p]),
     "omr_ntt_domain_info": (_c.c_int, [_c.c_void_p, _c.POINTER(_c.c_int), _c.POINTER(_c.c_uint64),
                                         _c.POINTER(_c.c_uint32), _c.POINTER(_c.c_uint64)]),
+    "omr_ntt_domain_check": (_c.c_int, [_c.c_void_p, _c.c_void_p]),
     "omr_ntt_domain_twiddles": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p]),
     "omr_ntt_encoder_name": (_c.c_char_p, [_c.c_int]),
     "omr_ntt_encoder_supports": (_c.c_int, [_c.c_int, _c.c_uint32]),

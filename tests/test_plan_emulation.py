@@ -62,3 +62,26 @@ def test_plan_errors():
     with pytest.raises(omr_ntt.OmrNttError):
         omr_ntt.plan_count(BabyBear, 28)  # > TWO_ADICITY
     assert omr_ntt.plan_count(TeddyBear, 30) >= 1
+
+
+def test_tma_pass_preconditions():
+    # the TMA-fed pass needs: column passes with a dense row pitch (es_in ==
+    # L_lo) and 16-byte rows; row passes with 16-byte aligned line starts and
+    # line lengths; tensor dimensions below 2^32
+    for field in (BabyBear, Goldilocks):
+        w = field.word_bytes
+        for log_n in range(16, 28):
+            for plan in range(omr_ntt.plan_count(field, log_n)):
+                for batch in (1, 64):
+                    for p in omr_ntt.plan_passes(field, log_n, plan, batch):
+                        T = 1 << p["logT"]
+                        if p["logT"] < 8 or p["twiddle"] == 0 and p["es_in"] != 1:
+                            continue
+                        if p["is_lo"] == 1:  # column pass
+                            assert p["es_in"] == p["L_lo"]
+                            assert (p["L_lo"] * w) % 16 == 0
+                            assert T * p["L_m"] * p["L_b"] < 2 ** 32
+                        else:  # row pass
+                            for stride in (p["is_lo"], p["is_m"], p["is_b"]):
+                                assert (stride * w) % 16 == 0
+                            assert (T * w) % 16 == 0
