@@ -60,54 +60,103 @@ constexpr bool has_tma_pass() {
 inline int effective_variant(int field, int mode, int logT, int variant) {
   if (variant <= 0 || mode == MODE_LINE || logT < 8) return 0;
   if (field != BABYBEAR && field != GOLDILOCKS) return 0;
-  return variant > 2 ? 2 : variant;
+  return 1;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 int device_sm_count(int dev);
 
-template <class F, int LOGT, int NTV, int MODE, bool INV>
-int launch_tma_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
+constexpr size_t kMaxDynSmem = 227 * 1024 - 1024;  // leaves room for the static mbarriers
+
+static inline CUresult encode_2d(CUtensorMap* map, int word, const void* base, uint64_t dim0,
+                                 uint64_t dim1, uint64_t pitch_words, uint32_t box0, uint32_t box1) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return CUDA_ERROR_NOT_SUPPORTED;
+  cuuint64_t dims[2] = {dim0, dim1};
+  cuuint64_t strides[1] = {pitch_words * (cuuint64_t)word};
+  cuuint32_t box[2] = {box0, box1};
+  cuuint32_t estr[2] = {1, 1};
+  return enc(map, word == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 2,
+             const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
+// Whether the pass geometry is dense enough for the 2-D TMA tensors of the
+// TMA pass (see issue_load / issue_store in ntt_pass_tma.cuh).
+template <class F>
+bool tma_geometry_ok(const PassArgs<F>& a, int logT, int mode) {
+  const uint64_t T = 1ull << logT, C = tma_cols<F>();
+  if ((reinterpret_cast<uintptr_t>(a.in) & 15) || (reinterpret_cast<uintptr_t>(a.out) & 15)) return false;
+  if (a.L_lo % C) return false;
+  if (mode == MODE_COL) {
+    const uint64_t rows = T * a.L_m * a.L_b;
+    return a.is_lo == 1 && a.os_lo == 1 && a.es_in == a.L_lo && a.es_out == a.L_lo &&
+           (a.L_m == 1 || (a.is_m == T * a.L_lo && a.os_m == T * a.L_lo)) &&
+           a.is_b == T * a.L_lo * a.L_m && a.os_b == a.is_b && rows < (1ull << 31);
+  }
+  if (mode == MODE_ROW) {
+    const uint64_t w = (uint64_t)a.L_lo * a.L_m;
+    return a.es_in == 1 && a.os_lo == 1 && (a.L_m == 1 || a.os_m == a.L_lo) && a.es_out == w &&
+           a.os_b == T * w && ((a.is_lo | a.is_m | a.is_b) * F::WORD) % 16 == 0 &&
+           T * a.L_b < (1ull << 31);
+  }
+  return false;
+}
+
+template <class F, int LOGT, int MODE, bool INV, bool TW>
+int launch_tma_k(const PassArgs<F>& a, int* err, uint32_t lo_n, uint32_t hi_n,
+                 cudaStream_t stream) {
   constexpr int C = tma_cols<F>();
-  constexpr int NT = tma_threads<F, LOGT, NTV>();
+  constexpr int NT = tma_threads<F, LOGT>();
   constexpr int T = 1 << LOGT;
-  constexpr size_t smem = tma_smem_bytes<F, LOGT, C>();
-  auto kern = ntt_tile_pass_tma<F, LOGT, C, NT, MODE, INV>;
-  static std::atomic<uint64_t> attr_set{0};
-  static std::atomic<int> occ_cache[64];
+  constexpr uint32_t BOX = T < 256 ? T : 256;
+  const size_t smem = tma_smem_total<F, LOGT, C>(lo_n, hi_n);
+  auto kern = ntt_tile_pass_tma<F, LOGT, C, NT, MODE, INV, TW>;
+  static std::atomic<size_t> attr_bytes[64];
   int dev = 0;
   cudaGetDevice(&dev);
-  const uint64_t bit = 1ull << (dev & 63);
-  if (!(attr_set.load() & bit)) {
-    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int occ = 0;
-    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
-    occ_cache[dev & 63] = occ < 1 ? 1 : occ;
-    attr_set.fetch_or(bit);
+  if (attr_bytes[dev & 63].load() < smem) {
+    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem));
+    attr_bytes[dev & 63] = kMaxDynSmem;
   }
-  const uint64_t groups = (a.L_lo + C - 1) / C;
-  const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * groups;
+  int occ = 0;
+  OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
+  if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "TMA pass does not fit on an SM");
+  const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
   if (ntiles == 0) return OMR_NTT_OK;
-  CUtensorMap map;
-  memset(&map, 0, sizeof(map));
+  CUtensorMap in_map, out_map;
+  memset(&in_map, 0, sizeof(in_map));
+  CUresult r;
   if constexpr (MODE == MODE_COL) {
-    auto enc = tensor_map_encoder();
-    if (!enc) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-    cuuint64_t dims[2] = {a.L_lo, (cuuint64_t)T * a.L_m * a.L_b};
-    cuuint64_t strides[1] = {(cuuint64_t)a.L_lo * F::WORD};
-    cuuint32_t box[2] = {(cuuint32_t)C, (cuuint32_t)(T < 256 ? T : 256)};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(&map, F::WORD == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32,
-                     2, const_cast<void*>(static_cast<const void*>(a.in)), dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    r = encode_2d(&in_map, F::WORD, a.in, a.L_lo, (uint64_t)T * a.L_m * a.L_b, a.L_lo, C, BOX);
+    if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (load) failed");
+    r = encode_2d(&out_map, F::WORD, a.out, a.L_lo, (uint64_t)T * a.L_m * a.L_b, a.L_lo, C, BOX);
+  } else {
+    const uint64_t w = (uint64_t)a.L_lo * a.L_m;
+    r = encode_2d(&out_map, F::WORD, a.out, w, (uint64_t)T * a.L_b, w, C, BOX);
   }
-  const uint64_t slots = (uint64_t)device_sm_count(dev) * occ_cache[dev & 63].load();
+  if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (store) failed");
+  const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
   const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
-  kern<<<grid, NT, smem, stream>>>(map, a, err);
+  kern<<<grid, NT, smem, stream>>>(in_map, out_map, a, err, lo_n, hi_n);
   OMR_CUDA_TRY(cudaGetLastError());
   return OMR_NTT_OK;
+}
+
+// Returns 1 ("not taken") when the geometry or the shared-memory budget does
+// not suit the TMA pass; the caller then runs variant 0.
+template <class F, int LOGT, int MODE, bool INV>
+int launch_tma_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
+  if (!tma_geometry_ok<F>(a, LOGT, MODE)) return 1;
+  if (a.tw_lo != nullptr) {
+    const uint32_t n = a.tw_mask + 1;
+    const uint32_t lo_n = n < (1u << kTwLoBits) ? n : (1u << kTwLoBits);
+    const uint32_t hi_n = n >> kTwLoBits ? n >> kTwLoBits : 1;
+    if (tma_smem_total<F, LOGT, tma_cols<F>()>(lo_n, hi_n) > kMaxDynSmem) return 1;
+    return launch_tma_k<F, LOGT, MODE, INV, true>(a, err, lo_n, hi_n, stream);
+  }
+  return launch_tma_k<F, LOGT, MODE, INV, false>(a, err, 0, 0, stream);
 }
 
 // Defined here, instantiated once per (field, mode, direction) in
@@ -117,20 +166,17 @@ template <class F, int MODE, bool INV>
 int launch_pass_dir(int logT, int variant, const PassArgs<F>& a, uint64_t blocks, int* err,
                     cudaStream_t s) {
   if constexpr (MODE != MODE_LINE && has_tma_pass<F>()) {
-    if (variant == 1 || variant == 2) {
-      switch (logT * 4 + variant) {
-        case 8 * 4 + 1: return launch_tma_t<F, 8, 0, MODE, INV>(a, err, s);
-        case 9 * 4 + 1: return launch_tma_t<F, 9, 0, MODE, INV>(a, err, s);
-        case 10 * 4 + 1: return launch_tma_t<F, 10, 0, MODE, INV>(a, err, s);
-        case 11 * 4 + 1: return launch_tma_t<F, 11, 0, MODE, INV>(a, err, s);
-        case 12 * 4 + 1: return launch_tma_t<F, 12, 0, MODE, INV>(a, err, s);
-        case 8 * 4 + 2: return launch_tma_t<F, 8, 1, MODE, INV>(a, err, s);
-        case 9 * 4 + 2: return launch_tma_t<F, 9, 1, MODE, INV>(a, err, s);
-        case 10 * 4 + 2: return launch_tma_t<F, 10, 1, MODE, INV>(a, err, s);
-        case 11 * 4 + 2: return launch_tma_t<F, 11, 1, MODE, INV>(a, err, s);
-        case 12 * 4 + 2: return launch_tma_t<F, 12, 1, MODE, INV>(a, err, s);
+    if (variant >= 1) {
+      int rc = 1;
+      switch (logT) {
+        case 8: rc = launch_tma_t<F, 8, MODE, INV>(a, err, s); break;
+        case 9: rc = launch_tma_t<F, 9, MODE, INV>(a, err, s); break;
+        case 10: rc = launch_tma_t<F, 10, MODE, INV>(a, err, s); break;
+        case 11: rc = launch_tma_t<F, 11, MODE, INV>(a, err, s); break;
+        case 12: rc = launch_tma_t<F, 12, MODE, INV>(a, err, s); break;
         default: break;
       }
+      if (rc != 1) return rc;
     }
   }
   return launch_pass_logt<F, MODE, INV, 0>(logT, a, blocks, s);
@@ -187,9 +233,7 @@ int launch_pass(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, cons
   a.tw_line_mul_m = p.tw_line_mul_m;
   a.has_scale = (inverse && last) ? 1 : 0;
   a.scale = F::make_tw(d->n_inv);
-  int variant = effective_variant(F::ID, p.mode, p.logT, p.variant);
-  if (variant && ((reinterpret_cast<uintptr_t>(in) & 15) || (p.mode == MODE_COL && p.es_in != p.L_lo)))
-    variant = 0;  // TMA needs 16-byte aligned sources and a dense row pitch
+  const int variant = effective_variant(F::ID, p.mode, p.logT, p.variant);
   a.L_b = p.L_b;
   const int C = tile_cols<F, 0>();
   const uint64_t blocks = p.L_b * (uint64_t)p.L_m * (uint64_t)((p.L_lo + C - 1) / C);

@@ -1,24 +1,29 @@
-// ntt_pass_tma.cuh -- persistent, double-buffered tile pass fed by TMA.
+// ntt_pass_tma.cuh -- persistent, double-buffered tile pass: TMA in, TMA out.
 //
-// Same arithmetic as ntt_tile_pass (ntt_pass.cuh), different data movement:
-//   * persistent CTAs walk the tiles of the pass (tile += gridDim.x);
+// Same arithmetic as ntt_tile_pass (ntt_pass.cuh), GB300 data movement:
+//   * persistent CTAs walk the tiles of a pass (tile += gridDim.x);
 //   * one elected thread lands the NEXT tile in the second shared-memory
 //     buffer while the whole CTA computes the current one:
 //       - column passes (adjacent lines adjacent in memory): 2-D TMA tiled
 //         loads (cp.async.bulk.tensor.2d) of [C columns x 256 rows] boxes;
 //       - row passes (a line is a contiguous run): one 1-D bulk copy
 //         (cp.async.bulk) per line;
-//     completion is tracked by an mbarrier per buffer (expect-tx bytes);
-//   * every wait is bounded: on timeout the CTA raises the domain's error
-//     word (read back as OMR_NTT_ERR_TIMEOUT), drains its own copies (again
-//     bounded) and exits;
-//   * rounds exchange through the landed buffer itself; the last round
-//     stores straight from registers (c-fast, one DRAM sector per 2 rows).
-// Shared-memory layouts (bank-conflict free for the c-fast warp mapping):
-//   landing, column pass: [t][c], row t at t*C words (TMA box layout);
-//   landing, row pass:    line c at c*(T + PAD) words, PAD = 128/(C*w) words;
-//   exchange:             [t'][c], t' = t ^ ((t >> logr0) & (RPB - 1)),
-//                         RPB = rows per 128-byte bank line.
+//     completion is tracked by one mbarrier per buffer (expect-tx bytes);
+//   * the radix-2^r Stockham rounds exchange through the landed buffer; the
+//     last round writes the results, four-step twiddle applied, into the same
+//     buffer in the [k][c] box layout and one thread stores the tile with 2-D
+//     TMA stores (cp.async.bulk.tensor ... global.shared::cta, bulk groups);
+//   * in-line roots and the four-step twiddle tables are staged in shared
+//     memory once per CTA; the four-step twiddles of one butterfly are a
+//     Montgomery chain base * step^q, so each output costs two products;
+//   * every wait is bounded: on timeout the CTA raises the domain's error word
+//     (read back as OMR_NTT_ERR_TIMEOUT), drains its own copies and exits.
+// Shared-memory layouts (c-fast warp mapping; bank-conflict free except a
+// 2-way conflict on the first exchange write):
+//   landing, column pass: [t][c]           word t*C + c          (TMA box)
+//   landing, row pass:    line c            word c*(T + PAD) + t, PAD = 128/(C*w)
+//   exchange:             [t][c] + padding  word t*C + c + (t >> 3)*XPAD, XPAD = 16/w
+//   staging (store):      [k][c]            word k*C + c          (TMA box)
 #pragma once
 #include <cuda.h>
 
@@ -64,6 +69,15 @@ OMR_D void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t
       "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
+OMR_D void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   map),
+               "r"(x), "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+OMR_D void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+OMR_D void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+OMR_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 OMR_D void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -72,42 +86,68 @@ OMR_D void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) 
       : "memory");
 }
 
+template <class F>
+constexpr int tma_cols() {
+  return 16 / F::WORD;  // 16-byte line groups: conflict-free layouts, two buffers fit
+}
 template <class F, int C>
 constexpr int land_pad() {
   return 128 / (C * F::WORD);  // words
 }
+template <class F>
+constexpr int xchg_pad() {
+  return 16 / F::WORD;  // words per 8 rows
+}
 template <class F, int LOGT, int C>
 constexpr size_t tma_buf_words() {
-  constexpr size_t a = (size_t)(1 << LOGT) * C;
-  constexpr size_t b = (size_t)C * ((1 << LOGT) + land_pad<F, C>());
-  return ((a > b ? a : b) * F::WORD + 1023) / 1024 * 1024 / F::WORD;  // 1 KiB aligned buffers
+  constexpr size_t T = (size_t)1 << LOGT;
+  constexpr size_t a = T * C + (T >> 3) * xchg_pad<F>();
+  constexpr size_t b = (size_t)C * (T + land_pad<F, C>());
+  return ((a > b ? a : b) * F::WORD + 127) / 128 * 128 / F::WORD;  // 128-byte aligned buffers
 }
 template <class F, int LOGT, int C>
 constexpr size_t tma_smem_bytes() {
-  return 2 * tma_buf_words<F, LOGT, C>() * F::WORD + 1024;  // + alignment slack
+  return 2 * tma_buf_words<F, LOGT, C>() * F::WORD + 128;  // + alignment slack
+}
+// plus the staged tables: roots (T) and, for twiddled passes, the four-step tables
+template <class F, int LOGT, int C>
+inline size_t tma_smem_total(uint32_t tw_lo_n, uint32_t tw_hi_n) {
+  return tma_smem_bytes<F, LOGT, C>() + ((size_t)(1 << LOGT) + tw_hi_n) * sizeof(typename F::Tw) +
+         (size_t)tw_lo_n * sizeof(typename F::E);
 }
 
-enum { LAND_COL = 0, LAND_ROW = 1, XCHG = 2 };
+enum { LAND_COL = 0, LAND_ROW = 1, XCHG = 2, STAGE = 3 };
 
 template <class F, int LOGT, int C, int LAYOUT>
 OMR_D int sidx(int t, int c) {
   constexpr int T = 1 << LOGT;
-  if constexpr (LAYOUT == LAND_COL) {
+  if constexpr (LAYOUT == LAND_COL || LAYOUT == STAGE) {
     return t * C + c;
   } else if constexpr (LAYOUT == LAND_ROW) {
     return c * (T + land_pad<F, C>()) + t;
   } else {
-    constexpr int ROWB = C * F::WORD;
-    constexpr int RPB = ROWB >= 128 ? 1 : 128 / ROWB;
-    constexpr int LOGR0 = RoundPlan<LOGT, max_radix_log<F>()>::logr(0);
-    return (t ^ ((t >> LOGR0) & (RPB - 1))) * C + c;
+    return t * C + c + (t >> 3) * xchg_pad<F>();
   }
+}
+
+// Twiddle tables staged in shared memory once per persistent CTA.
+template <class F>
+struct SmemTw {
+  const typename F::Tw* roots;  // omega_T^k, k < T
+  const typename F::E* lo;      // four-step table, low part (twiddle-Montgomery form)
+  const typename F::Tw* hi;     // four-step table, high part
+};
+
+// omega_N^e in twiddle-Montgomery form from the two-level table
+template <class F>
+OMR_D typename F::E tw_lookup(const SmemTw<F>& st, uint32_t e) {
+  return F::mul_tw(st.lo[e & ((1u << kTwLoBits) - 1)], st.hi[e >> kTwLoBits]);
 }
 
 template <class F, int LOGT, int C, int NT, int LOGR, int LOGNS, bool INV, int SRC, bool LAST,
           bool TW>
-OMR_D void tma_round(const PassArgs<F>& a, typename F::E* s, typename F::E* __restrict__ gout,
-                     int nvalid, uint32_t llo0, uint32_t lm) {
+OMR_D void tma_round(const PassArgs<F>& a, const SmemTw<F>& st, typename F::E* s, uint32_t llo0,
+                     uint32_t lm) {
   using E = typename F::E;
   constexpr int T = 1 << LOGT, R = 1 << LOGR, NS = 1 << LOGNS;
   constexpr int TR = T / R;
@@ -123,7 +163,7 @@ OMR_D void tma_round(const PassArgs<F>& a, typename F::E* s, typename F::E* __re
       for (int q = 0; q < R; q++) v[i][q] = s[sidx<F, LOGT, C, SRC>(j + q * TR, c)];
     }
   }
-  if constexpr (!LAST) __syncthreads();  // every read of the buffer precedes its overwrite
+  __syncthreads();  // every read of the buffer precedes its overwrite
 #pragma unroll
   for (int i = 0; i < PER; i++) {
     const int b = threadIdx.x + i * NT;
@@ -133,60 +173,68 @@ OMR_D void tma_round(const PassArgs<F>& a, typename F::E* s, typename F::E* __re
       if constexpr (LOGNS > 0) {
         constexpr int SCALE = T / (NS * R);
 #pragma unroll
-        for (int q = 1; q < R; q++)
-          v[i][q] = F::mul_tw(v[i][q], a.roots[(uint32_t)(q * jm * SCALE) * a.roots_stride]);
+        for (int q = 1; q < R; q++) v[i][q] = F::mul_tw(v[i][q], st.roots[q * jm * SCALE]);
       }
       dft_reg<F, LOGR, INV>(v[i]);
       const int d = ((j >> LOGNS) << (LOGNS + LOGR)) | jm;
+      if constexpr (!LAST) {
 #pragma unroll
-      for (int q = 0; q < R; q++) {
-        const int k = d + q * NS;
-        if constexpr (!LAST) {
-          s[sidx<F, LOGT, C, XCHG>(k, c)] = v[i][q];
-        } else {
-          if (c < nvalid) {
-            E y = v[i][q];
-            if constexpr (TW) {
-              if (a.tw_lo != nullptr) {
-                const uint32_t line = llo0 + (uint32_t)c + lm * a.tw_line_mul_m;
-                const uint32_t e = (line * (uint32_t)k * a.tw_scale) & a.tw_mask;
-                const E tm = F::mul_tw(a.tw_lo[e & ((1u << kTwLoBits) - 1)], a.tw_hi[e >> kTwLoBits]);
-                y = mul_m<F>(y, tm);
-              }
-            }
-            if (a.has_scale) y = F::mul_tw(y, a.scale);
-            gout[(uint32_t)c + (uint32_t)k * a.es_out] = y;
+        for (int q = 0; q < R; q++) s[sidx<F, LOGT, C, XCHG>(d + q * NS, c)] = v[i][q];
+      } else {
+        // outputs k = d + q * NS; four-step twiddle omega_N^(line k scale)
+        // = base * step^q, base = omega_N^(line d scale), step = omega_N^(line NS scale)
+        if constexpr (TW) {
+          const uint32_t ls = (llo0 + (uint32_t)c + lm * a.tw_line_mul_m) * a.tw_scale;
+          E w = tw_lookup<F>(st, (ls * (uint32_t)d) & a.tw_mask);
+          const E step = tw_lookup<F>(st, (ls * (uint32_t)NS) & a.tw_mask);
+#pragma unroll
+          for (int q = 0; q < R; q++) {
+            v[i][q] = mul_m<F>(v[i][q], w);
+            if (q + 1 < R) w = F::mont_mul(w, step);
           }
         }
+        if (a.has_scale) {
+#pragma unroll
+          for (int q = 0; q < R; q++) v[i][q] = F::mul_tw(v[i][q], a.scale);
+        }
+#pragma unroll
+        for (int q = 0; q < R; q++) s[sidx<F, LOGT, C, STAGE>(d + q * NS, c)] = v[i][q];
       }
     }
   }
   if constexpr (!LAST) __syncthreads();
 }
 
-template <class F, int LOGT, int C, int NT, int MODE, bool INV, int I>
-OMR_D void tma_rounds(const PassArgs<F>& a, typename F::E* s, typename F::E* gout, int nvalid,
-                      uint32_t llo0, uint32_t lm) {
+template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW, int I>
+OMR_D void tma_rounds(const PassArgs<F>& a, const SmemTw<F>& st, typename F::E* s, uint32_t llo0,
+                      uint32_t lm) {
   using RP = RoundPlan<LOGT, max_radix_log<F>()>;
   if constexpr (I < RP::ROUNDS) {
     constexpr int SRC = I == 0 ? (MODE == MODE_COL ? LAND_COL : LAND_ROW) : XCHG;
     constexpr bool LAST = I + 1 == RP::ROUNDS;
-    tma_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), INV, SRC, LAST, MODE == MODE_COL>(
-        a, s, gout, nvalid, llo0, lm);
-    tma_rounds<F, LOGT, C, NT, MODE, INV, I + 1>(a, s, gout, nvalid, llo0, lm);
+    tma_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), INV, SRC, LAST, TW>(a, st, s, llo0, lm);
+    tma_rounds<F, LOGT, C, NT, MODE, INV, TW, I + 1>(a, st, s, llo0, lm);
   }
 }
 
+template <class F, int C>
+OMR_D void tile_coords(const PassArgs<F>& a, uint64_t tile, uint32_t& g, uint32_t& lm,
+                       uint64_t& lb) {
+  const uint32_t groups = (a.L_lo + C - 1) / C;
+  g = (uint32_t)(tile % groups);
+  const uint64_t rest = tile / groups;
+  lm = (uint32_t)(rest % a.L_m);
+  lb = rest / a.L_m;
+}
+
 template <class F, int LOGT, int C, int MODE>
-OMR_D void issue_tile(const CUtensorMap* map, const PassArgs<F>& a, uint64_t tile,
+OMR_D void issue_load(const CUtensorMap* map, const PassArgs<F>& a, uint64_t tile,
                       typename F::E* buf, uint64_t* bar) {
   using E = typename F::E;
   constexpr int T = 1 << LOGT;
-  const uint32_t groups = (a.L_lo + C - 1) / C;
-  const uint32_t g = (uint32_t)(tile % groups);
-  const uint64_t rest = tile / groups;
-  const uint32_t lm = (uint32_t)(rest % a.L_m);
-  const uint64_t lb = rest / a.L_m;
+  uint32_t g, lm;
+  uint64_t lb;
+  tile_coords<F, C>(a, tile, g, lm, lb);
   if constexpr (MODE == MODE_COL) {
     constexpr int BOX = T < 256 ? T : 256;
     mbar_arrive_expect_tx(bar, (uint32_t)(T * C * F::WORD));
@@ -195,25 +243,54 @@ OMR_D void issue_tile(const CUtensorMap* map, const PassArgs<F>& a, uint64_t til
     for (int t0 = 0; t0 < T; t0 += BOX) tma_load_2d(buf + t0 * C, map, (int)(g * C), y0 + t0, bar);
   } else {
     const uint32_t llo0 = g * C;
-    const int nv = (int)min((uint32_t)C, a.L_lo - llo0);
     const E* src = a.in + (lb * a.is_b + lm * a.is_m + (uint64_t)llo0 * a.is_lo);
-    mbar_arrive_expect_tx(bar, (uint32_t)(nv * T * F::WORD));
+    mbar_arrive_expect_tx(bar, (uint32_t)(C * T * F::WORD));
 #pragma unroll 1
-    for (int c = 0; c < nv; c++)
+    for (int c = 0; c < C; c++)
       bulk_load(buf + c * (T + land_pad<F, C>()), src + (uint64_t)c * a.is_lo, T * F::WORD, bar);
   }
 }
 
-template <class F, int LOGT, int C, int NT, int MODE, bool INV>
+template <class F, int LOGT, int C, int MODE>
+OMR_D void issue_store(const CUtensorMap* map, const PassArgs<F>& a, uint64_t tile,
+                       const typename F::E* buf) {
+  constexpr int T = 1 << LOGT;
+  constexpr int BOX = T < 256 ? T : 256;
+  uint32_t g, lm;
+  uint64_t lb;
+  tile_coords<F, C>(a, tile, g, lm, lb);
+  int x, y0;
+  if constexpr (MODE == MODE_COL) {
+    x = (int)(g * C);
+    y0 = (int)((lb * a.L_m + lm) * (uint64_t)T);
+  } else {
+    x = (int)(g * C + lm * (uint32_t)a.os_m);
+    y0 = (int)(lb * (uint64_t)T);
+  }
+#pragma unroll 1
+  for (int t0 = 0; t0 < T; t0 += BOX) tma_store_2d(map, x, y0 + t0, buf + t0 * C);
+  bulk_commit();
+}
+
+// TW: the pass applies the four-step twiddle (column passes); its two tables
+// (tw_lo_n and tw_hi_n entries) are staged in shared memory behind the roots.
+template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW>
 __global__ void __launch_bounds__(NT, 1)
-    ntt_tile_pass_tma(const __grid_constant__ CUtensorMap map, const PassArgs<F> a, int* err) {
+    ntt_tile_pass_tma(const __grid_constant__ CUtensorMap in_map,
+                      const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err,
+                      uint32_t tw_lo_n, uint32_t tw_hi_n) {
   using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int T = 1 << LOGT;
   constexpr size_t BW = tma_buf_words<F, LOGT, C>();
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ int abort_flag;
-  E* base = reinterpret_cast<E*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  E* base = reinterpret_cast<E*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
   E* bufs[2] = {base, base + BW};
+  Tw* sroots = reinterpret_cast<Tw*>(base + 2 * BW);
+  Tw* shi = sroots + T;
+  E* slo = reinterpret_cast<E*>(shi + (TW ? tw_hi_n : 0));
 
   const uint32_t groups = (a.L_lo + C - 1) / C;
   const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * groups;
@@ -226,17 +303,33 @@ __global__ void __launch_bounds__(NT, 1)
   }
   __syncthreads();
   uint64_t tile = blockIdx.x;
+  bool outstanding[2] = {false, false};  // a load into the buffer has not been waited for
   if (threadIdx.x == 0) {
-    if (tile < ntiles) issue_tile<F, LOGT, C, MODE>(&map, a, tile, bufs[0], &bars[0]);
-    if (tile + gridDim.x < ntiles)
-      issue_tile<F, LOGT, C, MODE>(&map, a, tile + gridDim.x, bufs[1], &bars[1]);
+    if (tile < ntiles) {
+      issue_load<F, LOGT, C, MODE>(&in_map, a, tile, bufs[0], &bars[0]);
+      outstanding[0] = true;
+    }
+    if (tile + gridDim.x < ntiles) {
+      issue_load<F, LOGT, C, MODE>(&in_map, a, tile + gridDim.x, bufs[1], &bars[1]);
+      outstanding[1] = true;
+    }
   }
+  for (int k = threadIdx.x; k < T; k += NT) sroots[k] = a.roots[(uint32_t)k * a.roots_stride];
+  if constexpr (TW) {
+    for (uint32_t k = threadIdx.x; k < tw_hi_n; k += NT) shi[k] = a.tw_hi[k];
+    for (uint32_t k = threadIdx.x; k < tw_lo_n; k += NT) slo[k] = a.tw_lo[k];
+  }
+  const SmemTw<F> st{sroots, TW ? slo : nullptr, TW ? shi : nullptr};
+  // (the first loop iteration's barrier publishes the staged tables)
+
   uint32_t phase = 0;
   int it = 0;
   for (; tile < ntiles; tile += gridDim.x, it++) {
     const int b = it & 1;
     if (threadIdx.x == 0) {
-      if (!mbar_wait_bounded(&bars[b], (phase >> b) & 1)) {
+      if (mbar_wait_bounded(&bars[b], (phase >> b) & 1)) {
+        outstanding[b] = false;
+      } else {
         atomicExch(err, OMR_NTT_ERR_TIMEOUT);
         abort_flag = 1;
       }
@@ -244,43 +337,40 @@ __global__ void __launch_bounds__(NT, 1)
     __syncthreads();
     if (abort_flag) break;
     phase ^= 1u << b;
-    const uint32_t g = (uint32_t)(tile % groups);
-    const uint64_t rest = tile / groups;
-    const uint32_t lm = (uint32_t)(rest % a.L_m);
-    const uint64_t lb = rest / a.L_m;
-    const uint32_t llo0 = g * C;
-    const int nvalid = (int)min((uint32_t)C, a.L_lo - llo0);
-    E* gout = a.out + (lb * a.os_b + lm * a.os_m + (uint64_t)llo0 * a.os_lo);
-    tma_rounds<F, LOGT, C, NT, MODE, INV, 0>(a, bufs[b], gout, nvalid, llo0, lm);
-    __syncthreads();  // buffer b fully consumed
-    if (threadIdx.x == 0 && tile + 2ull * gridDim.x < ntiles) {
+    // buffer 1 - b held the previous tile: refill it with the next tile once
+    // that tile's TMA store has finished reading it
+    if (threadIdx.x == 0 && it > 0 && tile + gridDim.x < ntiles) {
+      bulk_wait_read_all();
       fence_proxy_async();
-      issue_tile<F, LOGT, C, MODE>(&map, a, tile + 2ull * gridDim.x, bufs[b], &bars[b]);
+      issue_load<F, LOGT, C, MODE>(&in_map, a, tile + gridDim.x, bufs[1 - b], &bars[1 - b]);
+      outstanding[1 - b] = true;
     }
+    uint32_t g, lm;
+    uint64_t lb;
+    tile_coords<F, C>(a, tile, g, lm, lb);
+    tma_rounds<F, LOGT, C, NT, MODE, INV, TW, 0>(a, st, bufs[b], g * C, lm);
+    fence_proxy_async();  // this thread's staging writes become visible to the TMA store
+    __syncthreads();
+    if (threadIdx.x == 0) issue_store<F, LOGT, C, MODE>(&out_map, a, tile, bufs[b]);
   }
-  if (abort_flag && threadIdx.x == 0) {
-    // drain this CTA's copies still in flight (bounded) before exiting
-    for (int k = 0; k < 2; k++) {
-      const uint64_t t = tile + (uint64_t)k * gridDim.x;
-      if (t < ntiles) mbar_wait_bounded(&bars[(it + k) & 1], (phase >> ((it + k) & 1)) & 1);
-    }
+  if (threadIdx.x == 0) {
+    bulk_wait_all();  // every store of this CTA has landed in global memory
+    // drain this CTA's loads still in flight (bounded) before exiting
+    for (int bb = 0; bb < 2; bb++)
+      if (outstanding[bb]) mbar_wait_bounded(&bars[bb], (phase >> bb) & 1);
   }
 }
 
-// Thread-count variants of the TMA pass: EPT elements per thread.
-template <class F, int NTV>
-constexpr int tma_ept() {
-  return F::WORD == 8 ? (NTV == 0 ? 16 : 8) : (NTV == 0 ? 32 : 16);
-}
+// Thread count of the TMA pass: EPT elements per thread.
 template <class F>
-constexpr int tma_cols() {
-  return 16 / F::WORD;  // 16-byte line groups: conflict-free layouts, two buffers fit
+constexpr int tma_ept() {
+  return F::WORD == 8 ? 16 : 32;
 }
-template <class F, int LOGT, int NTV>
+template <class F, int LOGT>
 constexpr int tma_threads() {
   constexpr int TC = (1 << LOGT) * tma_cols<F>();
-  constexpr int nt = TC / tma_ept<F, NTV>();
-  return nt < 32 ? 32 : (nt > 1024 ? 1024 : nt);
+  constexpr int nt = TC / tma_ept<F>();
+  return nt < 128 ? 128 : (nt > 1024 ? 1024 : nt);
 }
 
 }  // namespace omr
