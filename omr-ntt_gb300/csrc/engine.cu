@@ -150,7 +150,7 @@ std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
     std::vector<int> r(s.rbegin(), s.rend());
     if (r != s) splits.push_back(r);
   }
-  for (int v = 0; v < 2; v++)
+  for (int v = 0; v < 3; v++)
     for (auto& s : splits) {
       if (v > 0 && s.size() == 1) continue;  // single-pass plans have one kernel
       out.push_back(PlanShape{s, v});
@@ -268,7 +268,7 @@ static std::string plan_name(const PlanShape& s) {
     if (i) n += "x";
     n += std::to_string(1 << s.split[i]);
   }
-  if (s.split.size() > 1) n += s.variant == 0 ? " tile" : " tma";
+  if (s.split.size() > 1) n += s.variant == 0 ? " tile" : (s.variant == 1 ? " tma2buf" : " tma2cta");
   return n;
 }
 

@@ -60,7 +60,7 @@ constexpr bool has_tma_pass() {
 inline int effective_variant(int field, int mode, int logT, int variant) {
   if (variant <= 0 || mode == MODE_LINE || logT < 8) return 0;
   if (field != BABYBEAR && field != GOLDILOCKS) return 0;
-  return 1;
+  return variant > 2 ? 2 : variant;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
@@ -104,15 +104,15 @@ bool tma_geometry_ok(const PassArgs<F>& a, int logT, int mode) {
   return false;
 }
 
-template <class F, int LOGT, int MODE, bool INV, bool TW>
-int launch_tma_k(const PassArgs<F>& a, int* err, uint32_t lo_n, uint32_t hi_n,
-                 cudaStream_t stream) {
+template <class F, int LOGT, int MODE, bool INV, bool TW, int NBUF>
+int launch_tma_k(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   constexpr int C = tma_cols<F>();
-  constexpr int NT = tma_threads<F, LOGT>();
+  constexpr int NT = tma_threads<F, LOGT, NBUF>();
   constexpr int T = 1 << LOGT;
   constexpr uint32_t BOX = T < 256 ? T : 256;
-  const size_t smem = tma_smem_total<F, LOGT, C>(lo_n, hi_n);
-  auto kern = ntt_tile_pass_tma<F, LOGT, C, NT, MODE, INV, TW>;
+  constexpr size_t smem = tma_smem_total<F, LOGT, C, NBUF>();
+  static_assert(smem <= kMaxDynSmem, "TMA pass tile does not fit in shared memory");
+  auto kern = ntt_tile_pass_tma<F, LOGT, C, NT, MODE, INV, TW, NBUF>;
   static std::atomic<size_t> attr_bytes[64];
   int dev = 0;
   cudaGetDevice(&dev);
@@ -139,24 +139,18 @@ int launch_tma_k(const PassArgs<F>& a, int* err, uint32_t lo_n, uint32_t hi_n,
   if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (store) failed");
   const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
   const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
-  kern<<<grid, NT, smem, stream>>>(in_map, out_map, a, err, lo_n, hi_n);
+  kern<<<grid, NT, smem, stream>>>(in_map, out_map, a, err);
   OMR_CUDA_TRY(cudaGetLastError());
   return OMR_NTT_OK;
 }
 
 // Returns 1 ("not taken") when the geometry or the shared-memory budget does
 // not suit the TMA pass; the caller then runs variant 0.
-template <class F, int LOGT, int MODE, bool INV>
+template <class F, int LOGT, int MODE, bool INV, int NBUF>
 int launch_tma_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   if (!tma_geometry_ok<F>(a, LOGT, MODE)) return 1;
-  if (a.tw_lo != nullptr) {
-    const uint32_t n = a.tw_mask + 1;
-    const uint32_t lo_n = n < (1u << kTwLoBits) ? n : (1u << kTwLoBits);
-    const uint32_t hi_n = n >> kTwLoBits ? n >> kTwLoBits : 1;
-    if (tma_smem_total<F, LOGT, tma_cols<F>()>(lo_n, hi_n) > kMaxDynSmem) return 1;
-    return launch_tma_k<F, LOGT, MODE, INV, true>(a, err, lo_n, hi_n, stream);
-  }
-  return launch_tma_k<F, LOGT, MODE, INV, false>(a, err, 0, 0, stream);
+  if (a.tw_lo != nullptr) return launch_tma_k<F, LOGT, MODE, INV, true, NBUF>(a, err, stream);
+  return launch_tma_k<F, LOGT, MODE, INV, false, NBUF>(a, err, stream);
 }
 
 // Defined here, instantiated once per (field, mode, direction) in
@@ -168,12 +162,17 @@ int launch_pass_dir(int logT, int variant, const PassArgs<F>& a, uint64_t blocks
   if constexpr (MODE != MODE_LINE && has_tma_pass<F>()) {
     if (variant >= 1) {
       int rc = 1;
-      switch (logT) {
-        case 8: rc = launch_tma_t<F, 8, MODE, INV>(a, err, s); break;
-        case 9: rc = launch_tma_t<F, 9, MODE, INV>(a, err, s); break;
-        case 10: rc = launch_tma_t<F, 10, MODE, INV>(a, err, s); break;
-        case 11: rc = launch_tma_t<F, 11, MODE, INV>(a, err, s); break;
-        case 12: rc = launch_tma_t<F, 12, MODE, INV>(a, err, s); break;
+      switch (logT * 4 + variant) {
+        case 8 * 4 + 1: rc = launch_tma_t<F, 8, MODE, INV, 2>(a, err, s); break;
+        case 9 * 4 + 1: rc = launch_tma_t<F, 9, MODE, INV, 2>(a, err, s); break;
+        case 10 * 4 + 1: rc = launch_tma_t<F, 10, MODE, INV, 2>(a, err, s); break;
+        case 11 * 4 + 1: rc = launch_tma_t<F, 11, MODE, INV, 2>(a, err, s); break;
+        case 12 * 4 + 1: rc = launch_tma_t<F, 12, MODE, INV, 2>(a, err, s); break;
+        case 8 * 4 + 2: rc = launch_tma_t<F, 8, MODE, INV, 1>(a, err, s); break;
+        case 9 * 4 + 2: rc = launch_tma_t<F, 9, MODE, INV, 1>(a, err, s); break;
+        case 10 * 4 + 2: rc = launch_tma_t<F, 10, MODE, INV, 1>(a, err, s); break;
+        case 11 * 4 + 2: rc = launch_tma_t<F, 11, MODE, INV, 1>(a, err, s); break;
+        case 12 * 4 + 2: rc = launch_tma_t<F, 12, MODE, INV, 1>(a, err, s); break;
         default: break;
       }
       if (rc != 1) return rc;

@@ -13,7 +13,7 @@
 //     last round writes the results, four-step twiddle applied, into the same
 //     buffer in the [k][c] box layout and one thread stores the tile with 2-D
 //     TMA stores (cp.async.bulk.tensor ... global.shared::cta, bulk groups);
-//   * in-line roots and the four-step twiddle tables are staged in shared
+//   * per-round in-line twiddles and the four-step twiddle tables are staged in shared
 //     memory once per CTA; the four-step twiddles of one butterfly are a
 //     Montgomery chain base * step^q, so each output costs two products;
 //   * every wait is bounded: on timeout the CTA raises the domain's error word
@@ -96,25 +96,24 @@ constexpr int land_pad() {
 }
 template <class F>
 constexpr int xchg_pad() {
-  return 16 / F::WORD;  // words per 8 rows
+  return 16 / F::WORD;  // words per padding period
+}
+template <class F, int LOGT>
+constexpr int xchg_shift() {  // padding period: twice the first round's radix (rows)
+  return RoundPlan<LOGT, max_radix_log<F>()>::logr(0) + 1;
 }
 template <class F, int LOGT, int C>
 constexpr size_t tma_buf_words() {
   constexpr size_t T = (size_t)1 << LOGT;
-  constexpr size_t a = T * C + (T >> 3) * xchg_pad<F>();
+  constexpr size_t a = T * C + (T >> xchg_shift<F, LOGT>()) * xchg_pad<F>();
   constexpr size_t b = (size_t)C * (T + land_pad<F, C>());
   return ((a > b ? a : b) * F::WORD + 127) / 128 * 128 / F::WORD;  // 128-byte aligned buffers
 }
-template <class F, int LOGT, int C>
+template <class F, int LOGT, int C, int NBUF>
 constexpr size_t tma_smem_bytes() {
-  return 2 * tma_buf_words<F, LOGT, C>() * F::WORD + 128;  // + alignment slack
+  return NBUF * tma_buf_words<F, LOGT, C>() * F::WORD + 128;  // + alignment slack
 }
-// plus the staged tables: roots (T) and, for twiddled passes, the four-step tables
-template <class F, int LOGT, int C>
-inline size_t tma_smem_total(uint32_t tw_lo_n, uint32_t tw_hi_n) {
-  return tma_smem_bytes<F, LOGT, C>() + ((size_t)(1 << LOGT) + tw_hi_n) * sizeof(typename F::Tw) +
-         (size_t)tw_lo_n * sizeof(typename F::E);
-}
+
 
 enum { LAND_COL = 0, LAND_ROW = 1, XCHG = 2, STAGE = 3 };
 
@@ -126,26 +125,65 @@ OMR_D int sidx(int t, int c) {
   } else if constexpr (LAYOUT == LAND_ROW) {
     return c * (T + land_pad<F, C>()) + t;
   } else {
-    return t * C + c + (t >> 3) * xchg_pad<F>();
+    return t * C + c + (t >> xchg_shift<F, LOGT>()) * xchg_pad<F>();
   }
 }
 
-// Twiddle tables staged in shared memory once per persistent CTA.
+// Twiddle tables of the pass.
+//   rtw: the in-line twiddles of every round r > 0, staged in shared memory
+//        once per persistent CTA and laid out [q][jm] so that consecutive
+//        butterflies read consecutive words (round r starts at rtw_off(r);
+//        entry q*NS + jm = omega_T^(q jm T/(NS R)));
+//   lo/hi: the two-level four-step table in global memory (two lookups per
+//        16 outputs: the chain base and step).
 template <class F>
 struct SmemTw {
-  const typename F::Tw* roots;  // omega_T^k, k < T
-  const typename F::E* lo;      // four-step table, low part (twiddle-Montgomery form)
-  const typename F::Tw* hi;     // four-step table, high part
+  const typename F::Tw* rtw;
+  const typename F::E* __restrict__ lo;   // four-step table, low part (twiddle-Montgomery form)
+  const typename F::Tw* __restrict__ hi;  // four-step table, high part
 };
+
+template <int LOGT, int MAXR>
+constexpr int rtw_off(int r) {  // offset of round r's table (r >= 1)
+  int off = 0;
+  for (int k = 1; k < r; k++) off += (1 << RoundPlan<LOGT, MAXR>::logr(k)) << RoundPlan<LOGT, MAXR>::logns(k);
+  return off;
+}
+template <int LOGT, int MAXR>
+constexpr int rtw_size() {
+  return rtw_off<LOGT, MAXR>(RoundPlan<LOGT, MAXR>::ROUNDS);
+}
+// plus the staged per-round in-line twiddles (see SmemTw)
+template <class F, int LOGT, int C, int NBUF>
+constexpr size_t tma_smem_total() {
+  return tma_smem_bytes<F, LOGT, C, NBUF>() +
+         (size_t)rtw_size<LOGT, max_radix_log<F>()>() * sizeof(typename F::Tw);
+}
+
+template <class F, int LOGT, int RI>
+OMR_D void build_rtw(typename F::Tw* dst, const typename F::Tw* __restrict__ roots,
+                     uint32_t roots_stride, int nt) {
+  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  if constexpr (RI < RP::ROUNDS) {
+    if constexpr (RI >= 1) {
+      constexpr int R = 1 << RP::logr(RI), NS = 1 << RP::logns(RI);
+      constexpr int SCALE = (1 << LOGT) / (NS * R);
+      constexpr int OFF = rtw_off<LOGT, max_radix_log<F>()>(RI);
+      for (int k = threadIdx.x; k < R * NS; k += nt)
+        dst[OFF + k] = roots[(uint32_t)((k / NS) * (k % NS) * SCALE) * roots_stride];
+    }
+    build_rtw<F, LOGT, RI + 1>(dst, roots, roots_stride, nt);
+  }
+}
 
 // omega_N^e in twiddle-Montgomery form from the two-level table
 template <class F>
 OMR_D typename F::E tw_lookup(const SmemTw<F>& st, uint32_t e) {
-  return F::mul_tw(st.lo[e & ((1u << kTwLoBits) - 1)], st.hi[e >> kTwLoBits]);
+  return F::mul_tw(__ldg(&st.lo[e & ((1u << kTwLoBits) - 1)]), st.hi[e >> kTwLoBits]);
 }
 
-template <class F, int LOGT, int C, int NT, int LOGR, int LOGNS, bool INV, int SRC, bool LAST,
-          bool TW>
+template <class F, int LOGT, int C, int NT, int RI, int LOGR, int LOGNS, bool INV, int SRC,
+          bool LAST, bool TW>
 OMR_D void tma_round(const PassArgs<F>& a, const SmemTw<F>& st, typename F::E* s, uint32_t llo0,
                      uint32_t lm) {
   using E = typename F::E;
@@ -171,9 +209,9 @@ OMR_D void tma_round(const PassArgs<F>& a, const SmemTw<F>& st, typename F::E* s
       const int c = b % C, j = b / C;
       const int jm = j & (NS - 1);
       if constexpr (LOGNS > 0) {
-        constexpr int SCALE = T / (NS * R);
+        const typename F::Tw* tw = st.rtw + rtw_off<LOGT, max_radix_log<F>()>(RI) + jm;
 #pragma unroll
-        for (int q = 1; q < R; q++) v[i][q] = F::mul_tw(v[i][q], st.roots[q * jm * SCALE]);
+        for (int q = 1; q < R; q++) v[i][q] = F::mul_tw(v[i][q], tw[q * NS]);
       }
       dft_reg<F, LOGR, INV>(v[i]);
       const int d = ((j >> LOGNS) << (LOGNS + LOGR)) | jm;
@@ -205,15 +243,18 @@ OMR_D void tma_round(const PassArgs<F>& a, const SmemTw<F>& st, typename F::E* s
   if constexpr (!LAST) __syncthreads();
 }
 
-template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW, int I>
+// `between` runs (on every thread) after the barrier that ends the
+// second-to-last round: the producer uses it to refill the other buffer.
+template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW, int I, class Between>
 OMR_D void tma_rounds(const PassArgs<F>& a, const SmemTw<F>& st, typename F::E* s, uint32_t llo0,
-                      uint32_t lm) {
+                      uint32_t lm, Between&& between) {
   using RP = RoundPlan<LOGT, max_radix_log<F>()>;
   if constexpr (I < RP::ROUNDS) {
     constexpr int SRC = I == 0 ? (MODE == MODE_COL ? LAND_COL : LAND_ROW) : XCHG;
     constexpr bool LAST = I + 1 == RP::ROUNDS;
-    tma_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), INV, SRC, LAST, TW>(a, st, s, llo0, lm);
-    tma_rounds<F, LOGT, C, NT, MODE, INV, TW, I + 1>(a, st, s, llo0, lm);
+    tma_round<F, LOGT, C, NT, I, RP::logr(I), RP::logns(I), INV, SRC, LAST, TW>(a, st, s, llo0, lm);
+    if constexpr (I + 2 == RP::ROUNDS) between();
+    tma_rounds<F, LOGT, C, NT, MODE, INV, TW, I + 1>(a, st, s, llo0, lm, between);
   }
 }
 
@@ -272,25 +313,25 @@ OMR_D void issue_store(const CUtensorMap* map, const PassArgs<F>& a, uint64_t ti
   bulk_commit();
 }
 
-// TW: the pass applies the four-step twiddle (column passes); its two tables
-// (tw_lo_n and tw_hi_n entries) are staged in shared memory behind the roots.
-template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW>
-__global__ void __launch_bounds__(NT, 1)
+// TW: the pass applies the four-step twiddle (column passes).
+// NBUF = 2: one CTA per SM, the next tile lands while this one computes.
+// NBUF = 1: two CTAs per SM, each loads its next tile after storing the last;
+//           the other CTA keeps the SM busy meanwhile.
+template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW, int NBUF>
+__global__ void __launch_bounds__(NT, 3 - NBUF)
     ntt_tile_pass_tma(const __grid_constant__ CUtensorMap in_map,
-                      const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err,
-                      uint32_t tw_lo_n, uint32_t tw_hi_n) {
+                      const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
   using E = typename F::E;
   using Tw = typename F::Tw;
   constexpr int T = 1 << LOGT;
   constexpr size_t BW = tma_buf_words<F, LOGT, C>();
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ int abort_flag;
-  E* base = reinterpret_cast<E*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
-  E* bufs[2] = {base, base + BW};
-  Tw* sroots = reinterpret_cast<Tw*>(base + 2 * BW);
-  Tw* shi = sroots + T;
-  E* slo = reinterpret_cast<E*>(shi + (TW ? tw_hi_n : 0));
+  // align by pointer arithmetic on the shared array (keeps the state space)
+  E* base = reinterpret_cast<E*>(smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u));
+  E* bufs[2] = {base, base + (NBUF - 1) * BW};
+  Tw* srtw = reinterpret_cast<Tw*>(base + NBUF * BW);
 
   const uint32_t groups = (a.L_lo + C - 1) / C;
   const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * groups;
@@ -309,23 +350,19 @@ __global__ void __launch_bounds__(NT, 1)
       issue_load<F, LOGT, C, MODE>(&in_map, a, tile, bufs[0], &bars[0]);
       outstanding[0] = true;
     }
-    if (tile + gridDim.x < ntiles) {
+    if (NBUF == 2 && tile + gridDim.x < ntiles) {
       issue_load<F, LOGT, C, MODE>(&in_map, a, tile + gridDim.x, bufs[1], &bars[1]);
       outstanding[1] = true;
     }
   }
-  for (int k = threadIdx.x; k < T; k += NT) sroots[k] = a.roots[(uint32_t)k * a.roots_stride];
-  if constexpr (TW) {
-    for (uint32_t k = threadIdx.x; k < tw_hi_n; k += NT) shi[k] = a.tw_hi[k];
-    for (uint32_t k = threadIdx.x; k < tw_lo_n; k += NT) slo[k] = a.tw_lo[k];
-  }
-  const SmemTw<F> st{sroots, TW ? slo : nullptr, TW ? shi : nullptr};
+  build_rtw<F, LOGT, 1>(srtw, a.roots, a.roots_stride, NT);
+  const SmemTw<F> st{srtw, a.tw_lo, a.tw_hi};
   // (the first loop iteration's barrier publishes the staged tables)
 
   uint32_t phase = 0;
   int it = 0;
   for (; tile < ntiles; tile += gridDim.x, it++) {
-    const int b = it & 1;
+    const int b = NBUF == 2 ? (it & 1) : 0;
     if (threadIdx.x == 0) {
       if (mbar_wait_bounded(&bars[b], (phase >> b) & 1)) {
         outstanding[b] = false;
@@ -337,21 +374,32 @@ __global__ void __launch_bounds__(NT, 1)
     __syncthreads();
     if (abort_flag) break;
     phase ^= 1u << b;
-    // buffer 1 - b held the previous tile: refill it with the next tile once
-    // that tile's TMA store has finished reading it
-    if (threadIdx.x == 0 && it > 0 && tile + gridDim.x < ntiles) {
-      bulk_wait_read_all();
-      fence_proxy_async();
-      issue_load<F, LOGT, C, MODE>(&in_map, a, tile + gridDim.x, bufs[1 - b], &bars[1 - b]);
-      outstanding[1 - b] = true;
-    }
     uint32_t g, lm;
     uint64_t lb;
     tile_coords<F, C>(a, tile, g, lm, lb);
-    tma_rounds<F, LOGT, C, NT, MODE, INV, TW, 0>(a, st, bufs[b], g * C, lm);
+    // buffer 1 - b held the previous tile: refill it with the next tile once
+    // that tile's TMA store has finished reading it (by the second-to-last
+    // round it has, so the producer thread does not hold up the barriers)
+    auto refill = [&]() {
+      if (NBUF == 2 && threadIdx.x == 0 && it > 0 && tile + gridDim.x < ntiles) {
+        bulk_wait_read_all();
+        fence_proxy_async();
+        issue_load<F, LOGT, C, MODE>(&in_map, a, tile + gridDim.x, bufs[1 - b], &bars[1 - b]);
+        outstanding[1 - b] = true;
+      }
+    };
+    tma_rounds<F, LOGT, C, NT, MODE, INV, TW, 0>(a, st, bufs[b], g * C, lm, refill);
     fence_proxy_async();  // this thread's staging writes become visible to the TMA store
     __syncthreads();
-    if (threadIdx.x == 0) issue_store<F, LOGT, C, MODE>(&out_map, a, tile, bufs[b]);
+    if (threadIdx.x == 0) {
+      issue_store<F, LOGT, C, MODE>(&out_map, a, tile, bufs[b]);
+      if (NBUF == 1 && tile + gridDim.x < ntiles) {
+        bulk_wait_read_all();
+        fence_proxy_async();
+        issue_load<F, LOGT, C, MODE>(&in_map, a, tile + gridDim.x, bufs[0], &bars[0]);
+        outstanding[0] = true;
+      }
+    }
   }
   if (threadIdx.x == 0) {
     bulk_wait_all();  // every store of this CTA has landed in global memory
@@ -366,10 +414,10 @@ template <class F>
 constexpr int tma_ept() {
   return F::WORD == 8 ? 16 : 32;
 }
-template <class F, int LOGT>
+template <class F, int LOGT, int NBUF>
 constexpr int tma_threads() {
   constexpr int TC = (1 << LOGT) * tma_cols<F>();
-  constexpr int nt = TC / tma_ept<F>();
+  constexpr int nt = TC / (tma_ept<F>() * (3 - NBUF));
   return nt < 128 ? 128 : (nt > 1024 ? 1024 : nt);
 }
 
