@@ -147,6 +147,22 @@ int omr_ntt_forward(omr_ntt_domain_t d, int plan, const void *in, void *out, uin
 int omr_ntt_inverse(omr_ntt_domain_t d, int plan, const void *in, void *out, uint64_t batch,
                     void *stream);
 
+/* Forward NTT like omr_ntt_forward (default plan), for callers that must not
+ * allocate device memory during the call (for example a framework that has
+ * reserved all device memory for its own allocator, or a latency-bound loop
+ * that cannot afford the device-wide synchronisation a cudaMalloc/cudaFree
+ * can cause).  It calls no allocator: the multi-pass intermediate lives in a
+ * fixed 16 MiB array in device memory that the library declares statically
+ * (held by every GPU that loads the library until the process exits).
+ * N * batch * word_bytes above 16 MiB fails with OMR_NTT_ERR_CAPACITY.  All
+ * calls share that array: calls that overlap on the GPU race on it, so order
+ * them (one stream, or events).  The first call on each device looks up the
+ * array's device address; make it before any stream capture on that device.
+ * The domain is created beforehand (omr_ntt_domain_create allocates its
+ * tables).  No counterpart in the reference. */
+int omr_ntt_forward_noalloc(omr_ntt_domain_t d, const void *in, void *out, uint64_t batch,
+                            void *stream);
+
 /* Host-buffer forms of the two calls above (synchronous). */
 int omr_ntt_forward_host(omr_ntt_domain_t d, int plan, void *host_buf, uint64_t batch);
 int omr_ntt_inverse_host(omr_ntt_domain_t d, int plan, void *host_buf, uint64_t batch);

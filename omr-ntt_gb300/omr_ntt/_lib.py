@@ -53,6 +53,8 @@ _SIGS = {
                                     _c.c_void_p]),
     "omr_ntt_inverse": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p, _c.c_void_p, _c.c_uint64,
                                     _c.c_void_p]),
+    "omr_ntt_forward_noalloc": (_c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_uint64,
+                                            _c.c_void_p]),
     "omr_ntt_forward_host": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p, _c.c_uint64]),
     "omr_ntt_inverse_host": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p, _c.c_uint64]),
     "omr_ntt_partial": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_uint64, _c.c_void_p, _c.c_void_p,
