@@ -209,6 +209,42 @@ int omr_ntt_plan_passes(int field, uint32_t log_n, int plan, uint64_t batch, uin
 int omr_ntt_plan_run_pass(omr_ntt_domain_t d, int plan, int pass, int inverse, const void *src,
                           void *scratch, void *dst, uint64_t batch, void *stream);
 
+/* ---------------------------------------------------------------- planner */
+
+/* Candidate plans of a planning point (field, log2 N, output pattern, count;
+ * count == N or 0 means the full transform).  Each candidate is a strategy
+ * and a parameter: 0 full transform with plan `param`; 1 pruned prefix
+ * decomposition with line length 2^param; 2 strided fold then plan `param` of
+ * the count-point transform; 3 full plan `param` then gather.  Writes up to
+ * `cap` entries and returns the candidate count.  No GPU needed. */
+int omr_ntt_candidates(int field, uint32_t log_n, int pattern, uint64_t count, int *strategies,
+                       int *params, int cap);
+
+/* Run one candidate on device buffers: `batch` transforms of N words in
+ * `in`; full transforms write N words each, partial ones `count` words. */
+int omr_ntt_run_candidate(omr_ntt_domain_t d, int strategy, int param, int pattern,
+                          uint64_t count, const uint32_t *indices, const void *in, void *out,
+                          uint64_t batch, void *stream);
+
+/* Exhaustive autotuner: times every candidate of the planning point on
+ * buffers it allocates (seeded random canonical inputs, L2 flushed before each
+ * timed run, CUDA events); ms_out[i] = median ms of candidate i over `reps`.
+ * Returns the candidate count.  Setup-time tool: it allocates. */
+int omr_ntt_tune_point(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                       int reps, uint64_t seed, float *ms_out, int cap);
+
+/* Planner database (process-wide): the chosen candidate per planning point
+ * (batch and count bucketed to powers of two).  plan = -1 and the partial
+ * entry points consult it before the built-in heuristic.  get returns 1 if
+ * the point is known; load returns the number of entries read. */
+int omr_ntt_planner_set(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                        int strategy, int param);
+int omr_ntt_planner_get(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                        int *strategy, int *param);
+int omr_ntt_planner_clear(void);
+int omr_ntt_planner_save(const char *path);
+int omr_ntt_planner_load(const char *path);
+
 /* ---------------------------------------------------------------- misc */
 
 const char *omr_ntt_last_error(void);

@@ -255,10 +255,7 @@ std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanSha
 }
 
 int default_plan(int field, uint32_t log_n, uint64_t batch) {
-  (void)field;
-  (void)log_n;
-  (void)batch;
-  return 0;
+  return planned_full_plan(field, log_n, batch);
 }
 
 static std::string plan_name(const PlanShape& s) {

@@ -55,6 +55,8 @@ struct PlanShape {
 std::vector<PlanShape> enumerate_plans(uint32_t log_n);
 std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanShape& shape);
 int default_plan(int field, uint32_t log_n, uint64_t batch);
+// The planner's full-transform plan: planner database, else built-in heuristic (tuner.cu).
+int planned_full_plan(int field, uint32_t log_n, uint64_t batch);
 
 // ------------------------------------------------------------------ device tables
 // Per-field in-line roots omega_4096^k, k < 4096 (forward and inverse),
@@ -98,6 +100,9 @@ namespace omr {
 // Slot 0 is the transform passes' intermediate, slot 1 the partial-output
 // staging, slot 2 host-call staging.
 int domain_scratch(omr_ntt_domain_s* d, void* stream, size_t bytes, void** out, int slot = 0);
+
+// Number of SMs of device `dev` (cached).
+int device_sm_count(int dev);
 
 // The domain of size 2^log_m (same field), created on first use and owned by d.
 int sub_domain(omr_ntt_domain_s* d, uint32_t log_m, omr_ntt_domain_s** out);

@@ -64,7 +64,6 @@ inline int effective_variant(int field, int mode, int logT, int variant) {
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
-int device_sm_count(int dev);
 
 constexpr size_t kMaxDynSmem = 227 * 1024 - 1024;  // leaves room for the static mbarriers
 

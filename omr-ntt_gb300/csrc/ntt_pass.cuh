@@ -201,7 +201,7 @@ constexpr int tile_min_blocks() {
 }
 
 enum { SRC_GLOBAL = 0, SRC_SMEM = 1 };
-enum { DST_SMEM = 0, DST_GLOBAL = 1 };
+enum { DST_SMEM = 0, DST_GLOBAL = 1, DST_STAGE = 2 };  // STAGE: smem tile, four-step twiddle applied
 
 // One Stockham round.  SRC_GLOBAL reads the column-pass input directly (c-fast
 // mapping: 8 lines x 4 rows per warp, one sector per row); DST_GLOBAL writes
@@ -234,7 +234,7 @@ OMR_D void do_round(const PassArgs<F>& a, typename F::E* s, const typename F::E*
       }
     }
   }
-  if constexpr (SRC == SRC_SMEM && DST == DST_SMEM) __syncthreads();
+  if constexpr (SRC == SRC_SMEM && DST != DST_GLOBAL) __syncthreads();
 #pragma unroll
   for (int i = 0; i < PER; i++) {
     const int b = threadIdx.x + i * NT;
@@ -256,6 +256,18 @@ OMR_D void do_round(const PassArgs<F>& a, typename F::E* s, const typename F::E*
         const int k = d + q * NS;
         if constexpr (DST == DST_SMEM) {
           s[tile_idx<F, C>(k, c)] = v[i][q];
+        } else if constexpr (DST == DST_STAGE) {
+          E y = (E)0;
+          if (c < nvalid) {
+            y = v[i][q];
+            if constexpr (TW) {
+              const uint32_t line = llo0 + (uint32_t)c + lm * a.tw_line_mul_m;
+              const uint32_t e = (line * (uint32_t)k * a.tw_scale) & a.tw_mask;
+              const E tm = F::mul_tw(a.tw_lo[e & ((1u << kTwLoBits) - 1)], a.tw_hi[e >> kTwLoBits]);
+              y = mul_m<F>(y, tm);
+            }
+          }
+          s[tile_idx<F, C>(k, c)] = y;
         } else {
           if (c < nvalid) {
             E y = v[i][q];
@@ -277,7 +289,7 @@ OMR_D void do_round(const PassArgs<F>& a, typename F::E* s, const typename F::E*
       }
     }
   }
-  if constexpr (DST == DST_SMEM) __syncthreads();
+  if constexpr (DST != DST_GLOBAL) __syncthreads();
 }
 
 template <class F, int LOGT, int C, int NT, int MODE, bool INV, int I>

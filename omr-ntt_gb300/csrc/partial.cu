@@ -5,6 +5,161 @@
 
 namespace omr {
 
+// ---------------------------------------------------------------- prefix
+// Pruned prefix transform (the reference's TransformDecomposition,
+// src/encoders/transform_decomposition.rs:25-97, with n1 = T = next_pow2(m)):
+//   X[k] = sum_{r < N/T} omega_N^(r k) * DFT_T(x[r + (N/T) c] over c)[k],  k < m.
+// One persistent CTA walks groups of C adjacent columns r: T-point Stockham
+// rounds as in the tile pass (first round straight from global memory), the
+// last round leaves the twiddled outputs in shared memory, and each thread
+// adds its outputs k over the group's columns into registers.  A second
+// kernel sums the per-CTA rows.  The input is read once; m words are written.
+template <class F, int LOGT>
+constexpr int prefix_cols() {
+  constexpr int c = 4096 >> LOGT;
+  return c < 8 ? 8 : (c > 256 ? 256 : c);
+}
+template <class F, int LOGT>
+constexpr int prefix_threads() {
+  constexpr int tc = (1 << LOGT) * prefix_cols<F, LOGT>();
+  constexpr int nt = tc / (F::WORD == 8 ? 16 : 32);
+  return nt < 64 ? 64 : (nt > 512 ? 512 : nt);
+}
+
+template <class F, int LOGT, int C, int NT, int I>
+OMR_D void prefix_rounds(const PassArgs<F>& a, typename F::E* s, const typename F::E* gin,
+                         int nvalid, uint32_t llo0) {
+  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  if constexpr (I < RP::ROUNDS) {
+    constexpr int SRC = I == 0 ? SRC_GLOBAL : SRC_SMEM;
+    constexpr int DST = I + 1 == RP::ROUNDS ? DST_STAGE : DST_SMEM;
+    do_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), false, SRC, DST, false, true>(
+        a, s, gin, nullptr, nvalid, llo0, 0);
+    prefix_rounds<F, LOGT, C, NT, I + 1>(a, s, gin, nvalid, llo0);
+  }
+}
+
+template <class F, int LOGT>
+__global__ void __launch_bounds__(prefix_threads<F, LOGT>())
+    prefix_decomp_kernel(const PassArgs<F> a, uint32_t m, typename F::E* __restrict__ partial) {
+  using E = typename F::E;
+  constexpr int T = 1 << LOGT;
+  constexpr int C = prefix_cols<F, LOGT>();
+  constexpr int NT = prefix_threads<F, LOGT>();
+  constexpr int KPER = (T + NT - 1) / NT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  E* s = reinterpret_cast<E*>(smem_raw);
+  E acc[KPER];
+#pragma unroll
+  for (int i = 0; i < KPER; i++) acc[i] = 0;
+  const uint32_t groups = (a.L_lo + C - 1) / C;
+  for (uint32_t g = blockIdx.x; g < groups; g += gridDim.x) {
+    const uint32_t llo0 = g * C;
+    const int nvalid = (int)min((uint32_t)C, a.L_lo - llo0);
+    prefix_rounds<F, LOGT, C, NT, 0>(a, s, a.in + llo0, nvalid, llo0);
+#pragma unroll
+    for (int i = 0; i < KPER; i++) {
+      const int k = threadIdx.x + i * NT;
+      if (k < (int)m) {
+        E sum = acc[i];
+#pragma unroll 8
+        for (int c = 0; c < C; c++) sum = F::add(sum, s[tile_idx<F, C>(k, c)]);
+        acc[i] = sum;
+      }
+    }
+    __syncthreads();  // the next group's first round overwrites the tile
+  }
+#pragma unroll
+  for (int i = 0; i < KPER; i++) {
+    const int k = threadIdx.x + i * NT;
+    if (k < (int)m) partial[(uint64_t)blockIdx.x * m + k] = acc[i];
+  }
+}
+
+// out[k] = sum over rows of partial[row * m + k]
+template <class F>
+__global__ void sum_rows_kernel(const typename F::E* __restrict__ partial, uint32_t rows, uint32_t m,
+                                typename F::E* __restrict__ out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  typename F::E acc = 0;
+  for (uint32_t r = 0; r < rows; r++) acc = F::add(acc, partial[(uint64_t)r * m + k]);
+  out[k] = acc;
+}
+
+template <class F, int LOGT>
+static int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void* out,
+                           cudaStream_t stream) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int T = 1 << LOGT;
+  constexpr int C = prefix_cols<F, LOGT>();
+  constexpr int NT = prefix_threads<F, LOGT>();
+  constexpr size_t smem = (size_t)T * C * sizeof(E);
+  auto kern = prefix_decomp_kernel<F, LOGT>;
+  if (smem > 48 * 1024)
+    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RootTables rt;
+  int rc = get_root_tables(F::ID, &rt);
+  if (rc) return rc;
+  PassArgs<F> a{};
+  a.in = static_cast<const E*>(in);
+  a.L_lo = (uint32_t)(d->n >> LOGT);  // columns r
+  a.L_m = 1;
+  a.L_b = 1;
+  a.is_lo = 1;
+  a.es_in = (uint32_t)(d->n >> LOGT);
+  a.roots = static_cast<const Tw*>(rt.fwd);
+  a.roots_stride = 1u << (kMaxLogT - LOGT);
+  a.tw_lo = static_cast<const E*>(d->tw_lo_f);
+  a.tw_hi = static_cast<const Tw*>(d->tw_hi_f);
+  a.tw_scale = 1;
+  a.tw_mask = (uint32_t)(d->n - 1);
+  a.tw_line_mul_m = 0;
+  int occ = 0;
+  OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
+  int dev = 0;
+  OMR_CUDA_TRY(cudaGetDevice(&dev));
+  const uint32_t groups = (a.L_lo + C - 1) / C;
+  uint32_t grid = (uint32_t)device_sm_count(dev) * (uint32_t)(occ < 1 ? 1 : occ);
+  if (grid > groups) grid = groups;
+  void* part = nullptr;
+  rc = domain_scratch(d, stream, (size_t)grid * m * sizeof(E), &part, 1);
+  if (rc) return rc;
+  kern<<<grid, NT, smem, stream>>>(a, m, static_cast<E*>(part));
+  OMR_CUDA_TRY(cudaGetLastError());
+  sum_rows_kernel<F><<<(m + 255) / 256, 256, 0, stream>>>(static_cast<const E*>(part), grid, m,
+                                                           static_cast<E*>(out));
+  OMR_CUDA_TRY(cudaGetLastError());
+  return OMR_NTT_OK;
+}
+
+template <class F>
+static int launch_prefix(omr_ntt_domain_s* d, uint32_t m, int logt, const void* in, void* out,
+                         cudaStream_t stream) {
+  if (logt <= 0) {
+    logt = 0;
+    while ((1u << logt) < m) logt++;
+    if (logt == 0) logt = 1;
+  }
+  if ((1u << logt) < m || (uint32_t)logt > d->log_n) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "decomposition line shorter than the prefix");
+  switch (logt) {
+    case 1: return launch_prefix_t<F, 1>(d, m, in, out, stream);
+    case 2: return launch_prefix_t<F, 2>(d, m, in, out, stream);
+    case 3: return launch_prefix_t<F, 3>(d, m, in, out, stream);
+    case 4: return launch_prefix_t<F, 4>(d, m, in, out, stream);
+    case 5: return launch_prefix_t<F, 5>(d, m, in, out, stream);
+    case 6: return launch_prefix_t<F, 6>(d, m, in, out, stream);
+    case 7: return launch_prefix_t<F, 7>(d, m, in, out, stream);
+    case 8: return launch_prefix_t<F, 8>(d, m, in, out, stream);
+    case 9: return launch_prefix_t<F, 9>(d, m, in, out, stream);
+    case 10: return launch_prefix_t<F, 10>(d, m, in, out, stream);
+    case 11: return launch_prefix_t<F, 11>(d, m, in, out, stream);
+    case 12: return launch_prefix_t<F, 12>(d, m, in, out, stream);
+  }
+  return fail(OMR_NTT_ERR_SIZE, "prefix decomposition needs m <= 4096");
+}
+
 // out[j] = full[sel(j)]; out-of-range indices produce 0 (never an OOB read).
 template <class F>
 __global__ void gather_kernel(const typename F::E* __restrict__ full, uint64_t n, int pattern,
@@ -56,49 +211,96 @@ static int launch_colsum(const typename F::E* x, uint64_t rows, uint64_t cols,
   return OMR_NTT_OK;
 }
 
+enum { STRAT_DECOMP_ = 1, STRAT_FOLD_ = 2, STRAT_GATHER_ = 3 };
+
 template <class F>
-int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uint32_t* indices,
-                     const void* in, void* out, cudaStream_t stream) {
+static int run_fold(omr_ntt_domain_s* d, int sub_plan, uint64_t count, const void* in, void* out,
+                    cudaStream_t stream) {
   using E = typename F::E;
   const size_t w = sizeof(E);
-  const uint64_t n = d->n;
-  if (pattern == OMR_NTT_PATTERN_STRIDED && count < n) {
-    // fold: y[n'] = sum_q x[n' + count q], then X[j N/count] = DFT_count(y)[j]
-    uint32_t log_s = 0;
-    while ((1ull << log_s) < count) log_s++;
-    omr_ntt_domain_s* sd = nullptr;
-    int rc = sub_domain(d, log_s, &sd);
-    if (rc) return rc;
-    const uint64_t rows = n / count;
-    // staging: first-level partial sums (<= 4096 chunks) then y
-    const uint64_t max_chunks = 4096;
-    void* buf = nullptr;
-    rc = domain_scratch(d, stream, (size_t)(max_chunks + 1) * count * w, &buf, 1);
-    if (rc) return rc;
-    E* part = static_cast<E*>(buf);
-    uint64_t nch = 0;
-    rc = launch_colsum<F>(static_cast<const E*>(in), rows, count, part, max_chunks, &nch, stream);
-    if (rc) return rc;
-    E* y = part;
-    if (nch > 1) {
-      y = part + nch * count;
-      uint64_t one = 0;
-      rc = launch_colsum<F>(part, nch, count, y, 1, &one, stream);
-      if (rc) return rc;
-    }
-    return run_transform(sd, -1, false, y, out, 1, stream);
-  }
-  // full transform into scratch, then gather
-  void* full = nullptr;
-  int rc = domain_scratch(d, stream, (size_t)n * w, &full, 1);
+  // fold: y[n'] = sum_q x[n' + count q], then X[j N/count] = DFT_count(y)[j]
+  uint32_t log_s = 0;
+  while ((1ull << log_s) < count) log_s++;
+  omr_ntt_domain_s* sd = nullptr;
+  int rc = sub_domain(d, log_s, &sd);
   if (rc) return rc;
-  rc = run_transform(d, -1, false, in, full, 1, stream);
+  const uint64_t rows = d->n / count;
+  const uint64_t max_chunks = 4096;  // first-level partial sums, then y
+  void* buf = nullptr;
+  rc = domain_scratch(d, stream, (size_t)(max_chunks + 1) * count * w, &buf, 1);
+  if (rc) return rc;
+  E* part = static_cast<E*>(buf);
+  uint64_t nch = 0;
+  rc = launch_colsum<F>(static_cast<const E*>(in), rows, count, part, max_chunks, &nch, stream);
+  if (rc) return rc;
+  E* y = part;
+  if (nch > 1) {
+    y = part + nch * count;
+    uint64_t one = 0;
+    rc = launch_colsum<F>(part, nch, count, y, 1, &one, stream);
+    if (rc) return rc;
+  }
+  return run_transform(sd, sub_plan, false, y, out, 1, stream);
+}
+
+template <class F>
+static int run_gather(omr_ntt_domain_s* d, int plan, int pattern, uint64_t count,
+                      const uint32_t* indices, const void* in, void* out, cudaStream_t stream) {
+  using E = typename F::E;
+  void* full = nullptr;
+  int rc = domain_scratch(d, stream, (size_t)d->n * sizeof(E), &full, 1);
+  if (rc) return rc;
+  rc = run_transform(d, plan, false, in, full, 1, stream);
   if (rc) return rc;
   unsigned blocks = (unsigned)((count + 255) / 256);
-  gather_kernel<F><<<blocks, 256, 0, stream>>>(static_cast<const E*>(full), n, pattern, count,
+  gather_kernel<F><<<blocks, 256, 0, stream>>>(static_cast<const E*>(full), d->n, pattern, count,
                                               indices, static_cast<E*>(out));
   OMR_CUDA_TRY(cudaGetLastError());
   return OMR_NTT_OK;
+}
+
+template <class F>
+static int run_strategy_t(omr_ntt_domain_s* d, int strategy, int param, int pattern,
+                          uint64_t count, const uint32_t* indices, const void* in, void* out,
+                          cudaStream_t stream) {
+  const uint64_t n = d->n;
+  switch (strategy) {
+    case STRAT_DECOMP_:
+      if (pattern != OMR_NTT_PATTERN_PREFIX || count > 4096 || count >= n)
+        return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "decomposition serves prefixes of <= 4096 outputs");
+      return launch_prefix<F>(d, (uint32_t)count, param, in, out, stream);
+    case STRAT_FOLD_:
+      if (pattern != OMR_NTT_PATTERN_STRIDED || count >= n)
+        return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "fold serves strided patterns");
+      return run_fold<F>(d, param, count, in, out, stream);
+    case STRAT_GATHER_:
+      return run_gather<F>(d, param, pattern, count, indices, in, out, stream);
+  }
+  return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown partial strategy");
+}
+
+int run_partial_strategy(omr_ntt_domain_s* d, int strategy, int param, int pattern,
+                         uint64_t count, const uint32_t* indices, const void* in, void* out,
+                         cudaStream_t stream) {
+  return with_field(d->field, [&](auto f) {
+    return run_strategy_t<decltype(f)>(d, strategy, param, pattern, count, indices, in, out,
+                                       stream);
+  });
+}
+
+template <class F>
+int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uint32_t* indices,
+                     const void* in, void* out, cudaStream_t stream) {
+  const uint64_t n = d->n;
+  int strategy = 0, param = 0;
+  if (omr_ntt_planner_get(d->field, d->log_n, 1, pattern, count, &strategy, &param) == 1 &&
+      strategy >= STRAT_DECOMP_ && strategy <= STRAT_GATHER_)
+    return run_strategy_t<F>(d, strategy, param, pattern, count, indices, in, out, stream);
+  if (pattern == OMR_NTT_PATTERN_STRIDED && count < n)
+    return run_fold<F>(d, -1, count, in, out, stream);
+  if (pattern == OMR_NTT_PATTERN_PREFIX && count <= 4096 && count < n && n / count >= 2)
+    return launch_prefix<F>(d, (uint32_t)count, 0, in, out, stream);
+  return run_gather<F>(d, -1, pattern, count, indices, in, out, stream);
 }
 
 template int partial_dispatch<BabyBear>(omr_ntt_domain_s*, int, uint64_t, const uint32_t*,

@@ -23,6 +23,12 @@ namespace omr {
 int run_partial(omr_ntt_domain_s* d, int pattern, uint64_t count, const uint32_t* indices,
                 const void* in, void* out, cudaStream_t stream);
 
+// One explicit partial strategy (1 decomposition with line 2^param, 2 strided
+// fold with sub-plan param, 3 full plan param + gather).
+int run_partial_strategy(omr_ntt_domain_s* d, int strategy, int param, int pattern,
+                         uint64_t count, const uint32_t* indices, const void* in, void* out,
+                         cudaStream_t stream);
+
 template <class F>
 int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uint32_t* indices,
                      const void* in, void* out, cudaStream_t stream);

@@ -1,0 +1,317 @@
+// tuner.cu -- plan candidates, the exhaustive autotuner and the planner database.
+//
+// A planning point is (field, log2 N, batch, output pattern, output count).
+// Its candidate plans are
+//   * full transforms  (count == N): every pass split x kernel variant of
+//     enumerate_plans (engine.cu);
+//   * partial outputs: the pruned prefix decomposition for each line length
+//     T >= count (T <= 4096), the strided fold + every plan of the count-point
+//     transform, and every full plan followed by a gather.
+// omr_ntt_tune_point times every candidate on device buffers it owns (CUDA
+// events, L2 flushed before each timed run, median of `reps`); the caller
+// records the fastest in the planner database (omr_ntt_planner_*), which the
+// planner (plan = -1) consults before its built-in heuristic.  All candidates
+// are exact, so the choice changes speed, never a result.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "partial.cuh"
+
+namespace omr {
+
+enum Strategy : int { STRAT_FULL = 0, STRAT_DECOMP = 1, STRAT_FOLD = 2, STRAT_GATHER = 3 };
+
+struct Cand {
+  int strategy;
+  int param;  // full/gather: plan id; decomp: log2 T; fold: plan id of the count-point transform
+};
+
+static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint64_t count) {
+  (void)field;
+  std::vector<Cand> v;
+  const uint64_t n = 1ull << log_n;
+  const int nfull = (int)enumerate_plans(log_n).size();
+  if (count >= n || count == 0) {
+    for (int p = 0; p < nfull; p++) v.push_back({STRAT_FULL, p});
+    return v;
+  }
+  if (pattern == OMR_NTT_PATTERN_PREFIX) {
+    int lt = 0;
+    while ((1ull << lt) < count) lt++;
+    if (lt == 0) lt = 1;
+    for (int t = lt; t <= kMaxLogT && (uint32_t)t < log_n; t++) v.push_back({STRAT_DECOMP, t});
+  }
+  if (pattern == OMR_NTT_PATTERN_STRIDED && (count & (count - 1)) == 0) {
+    uint32_t ls = 0;
+    while ((1ull << ls) < count) ls++;
+    const int nsub = (int)enumerate_plans(ls).size();
+    for (int p = 0; p < nsub; p++) v.push_back({STRAT_FOLD, p});
+  }
+  for (int p = 0; p < nfull; p++) v.push_back({STRAT_GATHER, p});
+  return v;
+}
+
+// ------------------------------------------------------------------ planner DB
+struct Key {
+  int field, log_n, batch_log, pattern, count_log;
+  bool operator<(const Key& o) const {
+    return std::tie(field, log_n, batch_log, pattern, count_log) <
+           std::tie(o.field, o.log_n, o.batch_log, o.pattern, o.count_log);
+  }
+};
+static std::mutex g_db_mu;
+static std::map<Key, Cand> g_db;
+
+static int ilog2_ceil(uint64_t x) {
+  int l = 0;
+  while ((1ull << l) < x) l++;
+  return l;
+}
+
+static Key make_key(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count) {
+  const uint64_t n = 1ull << log_n;
+  if (count >= n || count == 0) pattern = -1;  // full transform
+  return Key{field, (int)log_n, ilog2_ceil(batch ? batch : 1), pattern,
+             pattern < 0 ? (int)log_n : ilog2_ceil(count)};
+}
+
+static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                      Cand* out) {
+  std::lock_guard<std::mutex> lk(g_db_mu);
+  auto it = g_db.find(make_key(field, log_n, batch, pattern, count));
+  if (it == g_db.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+// Built-in heuristic (measured on GB300): the two-buffer TMA pass for the
+// headline fields' balanced split, the tile pass otherwise.
+static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
+  (void)batch;
+  const auto plans = enumerate_plans(log_n);
+  if (plans.size() <= 1 || plans[0].split.size() < 2) return 0;
+  if (field != BABYBEAR && field != GOLDILOCKS) return 0;
+  size_t nsplit = 0;
+  for (auto& p : plans)
+    if (p.variant == 0) nsplit++;
+  const int cand = (int)nsplit;  // variant 1, first (balanced) split
+  return cand < (int)plans.size() ? cand : 0;
+}
+
+int planned_full_plan(int field, uint32_t log_n, uint64_t batch) {
+  Cand c;
+  const int n = (int)enumerate_plans(log_n).size();
+  if (db_lookup(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
+    return c.param;
+  return heuristic_full_plan(field, log_n, batch);
+}
+
+// ------------------------------------------------------------------ executors
+int run_partial_strategy(omr_ntt_domain_s* d, int strategy, int param, int pattern,
+                         uint64_t count, const uint32_t* indices, const void* in, void* out,
+                         cudaStream_t stream);
+
+static int run_candidate(omr_ntt_domain_s* d, const Cand& c, int pattern, uint64_t count,
+                         const uint32_t* indices, const void* in, void* out, uint64_t batch,
+                         cudaStream_t stream) {
+  if (c.strategy == STRAT_FULL) return run_transform(d, c.param, false, in, out, batch, stream);
+  const size_t w = word_bytes(d->field);
+  for (uint64_t b = 0; b < batch; b++) {
+    int rc = run_partial_strategy(d, c.strategy, c.param, pattern, count, indices,
+                                  static_cast<const char*>(in) + b * d->n * w,
+                                  static_cast<char*>(out) + b * count * w, stream);
+    if (rc) return rc;
+  }
+  return OMR_NTT_OK;
+}
+
+template <class F>
+__global__ void fill_random_kernel(typename F::E* x, uint64_t n, uint64_t seed) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    x[i] = (typename F::E)(z % F::p64());
+  }
+}
+
+}  // namespace omr
+
+using namespace omr;
+
+extern "C" {
+
+// Planner database -----------------------------------------------------------
+
+int omr_ntt_planner_set(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                        int strategy, int param) {
+  if (!valid_field(field) || (int)log_n > two_adicity(field))
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "bad field or size");
+  std::lock_guard<std::mutex> lk(g_db_mu);
+  g_db[make_key(field, log_n, batch, pattern, count)] = Cand{strategy, param};
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_planner_get(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                        int* strategy, int* param) {
+  Cand c;
+  if (!db_lookup(field, log_n, batch, pattern, count, &c)) return 0;
+  if (strategy) *strategy = c.strategy;
+  if (param) *param = c.param;
+  return 1;
+}
+
+int omr_ntt_planner_clear(void) {
+  std::lock_guard<std::mutex> lk(g_db_mu);
+  g_db.clear();
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_planner_save(const char* path) {
+  if (!path) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null path");
+  std::lock_guard<std::mutex> lk(g_db_mu);
+  std::ofstream f(path);
+  if (!f) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+  f << "# omr-ntt planner db: field log_n batch_log pattern count_log strategy param\n";
+  for (auto& kv : g_db)
+    f << kv.first.field << ' ' << kv.first.log_n << ' ' << kv.first.batch_log << ' '
+      << kv.first.pattern << ' ' << kv.first.count_log << ' ' << kv.second.strategy << ' '
+      << kv.second.param << '\n';
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_planner_load(const char* path) {
+  if (!path) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null path");
+  std::ifstream f(path);
+  if (!f) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+  std::lock_guard<std::mutex> lk(g_db_mu);
+  std::string line;
+  int n = 0;
+  while (std::getline(f, line)) {
+    if (line.empty() || line[0] == '#') continue;
+    std::istringstream is(line);
+    Key k;
+    Cand c;
+    if (is >> k.field >> k.log_n >> k.batch_log >> k.pattern >> k.count_log >> c.strategy >> c.param) {
+      g_db[k] = c;
+      n++;
+    }
+  }
+  return n;
+}
+
+// Candidates -----------------------------------------------------------------
+
+int omr_ntt_candidates(int field, uint32_t log_n, int pattern, uint64_t count, int* strategies,
+                       int* params, int cap) {
+  if (!valid_field(field) || (int)log_n > two_adicity(field))
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "bad field or size");
+  auto v = candidates(field, log_n, pattern, count);
+  for (int i = 0; i < (int)v.size() && i < cap; i++) {
+    if (strategies) strategies[i] = v[i].strategy;
+    if (params) params[i] = v[i].param;
+  }
+  return (int)v.size();
+}
+
+// Run one candidate on device buffers (batch transforms; partial outputs
+// are written `count` words per transform).
+int omr_ntt_run_candidate(omr_ntt_domain_t d, int strategy, int param, int pattern, uint64_t count,
+                          const uint32_t* indices, const void* in, void* out, uint64_t batch,
+                          void* stream) {
+  if (!d || !in || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  DeviceGuard g(d->device);
+  return run_candidate(d, Cand{strategy, param}, pattern, count, indices, in, out, batch,
+                       (cudaStream_t)stream);
+}
+
+// Time every candidate of the planning point; ms_out[i] = median ms of
+// candidate i over `reps` runs (L2 flushed before each).  Returns the number
+// of candidates (or a negative status).
+int omr_ntt_tune_point(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                       int reps, uint64_t seed, float* ms_out, int cap) {
+  if (!valid_field(field) || (int)log_n > two_adicity(field) || batch == 0 || reps < 1)
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "bad tuning point");
+  omr_ntt_domain_t d = nullptr;
+  int rc = omr_ntt_domain_create(field, log_n, &d);
+  if (rc) return rc;
+  const uint64_t n = 1ull << log_n;
+  const bool full = count >= n || count == 0;
+  const uint64_t outw = full ? n : count;
+  const size_t w = word_bytes(field);
+  auto cands = candidates(field, log_n, pattern, count);
+  void *in = nullptr, *out = nullptr, *flush = nullptr;
+  uint32_t* idx = nullptr;
+  const size_t flush_bytes = 256ull << 20;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(in);
+    cudaFree(out);
+    cudaFree(flush);
+    cudaFree(idx);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    omr_ntt_domain_destroy(d);
+  };
+  if (cudaMalloc(&in, n * batch * w) != cudaSuccess || cudaMalloc(&out, outw * batch * w) != cudaSuccess ||
+      cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+    cleanup();
+    return fail(OMR_NTT_ERR_ALLOC, "tuning buffers");
+  }
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cleanup();
+    return fail(OMR_NTT_ERR_CUDA, "tuning stream/events");
+  }
+  rc = with_field(field, [&](auto f) -> int {
+    using F = decltype(f);
+    fill_random_kernel<F><<<1024, 256, 0, st>>>(static_cast<typename F::E*>(in), n * batch, seed);
+    return cudaGetLastError() == cudaSuccess ? OMR_NTT_OK : OMR_NTT_ERR_CUDA;
+  });
+  if (!rc && pattern == OMR_NTT_PATTERN_INDICES && !full) {
+    // seeded distinct indices: a stride coprime to N walks a permutation
+    std::vector<uint32_t> h(count);
+    uint64_t stride = (seed * 2654435761ull) | 1ull, off = seed % n;
+    for (uint64_t j = 0; j < count; j++) h[j] = (uint32_t)((off + j * stride) & (n - 1));
+    if (cudaMalloc(&idx, count * 4) != cudaSuccess ||
+        cudaMemcpy(idx, h.data(), count * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = fail(OMR_NTT_ERR_ALLOC, "tuning indices");
+  }
+  for (int i = 0; !rc && i < (int)cands.size(); i++) {
+    // warm-up (also builds sub-domains and scratch outside the timed runs)
+    rc = run_candidate(d, cands[i], pattern, count, idx, in, out, batch, st);
+    if (rc) break;
+    std::vector<float> t;
+    for (int r = 0; r < reps && !rc; r++) {
+      cudaMemsetAsync(flush, r & 0xff, flush_bytes, st);
+      cudaEventRecord(e0, st);
+      rc = run_candidate(d, cands[i], pattern, count, idx, in, out, batch, st);
+      cudaEventRecord(e1, st);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(OMR_NTT_ERR_CUDA, "tuning sync");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      t.push_back(ms);
+    }
+    std::sort(t.begin(), t.end());
+    if (i < cap && ms_out) ms_out[i] = t.empty() ? -1.f : t[t.size() / 2];
+  }
+  if (!rc) rc = omr_ntt_domain_check(d, st);
+  cleanup();
+  return rc ? rc : (int)cands.size();
+}
+
+}  // extern "C"

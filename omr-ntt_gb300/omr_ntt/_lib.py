@@ -68,6 +68,20 @@ _SIGS = {
                                         _c.POINTER(_c.c_uint64), _c.c_int]),
     "omr_ntt_plan_run_pass": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_int, _c.c_int, _c.c_void_p,
                                           _c.c_void_p, _c.c_void_p, _c.c_uint64, _c.c_void_p]),
+    "omr_ntt_candidates": (_c.c_int, [_c.c_int, _c.c_uint32, _c.c_int, _c.c_uint64,
+                                       _c.POINTER(_c.c_int), _c.POINTER(_c.c_int), _c.c_int]),
+    "omr_ntt_run_candidate": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_int, _c.c_int, _c.c_uint64,
+                                          _c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_uint64,
+                                          _c.c_void_p]),
+    "omr_ntt_tune_point": (_c.c_int, [_c.c_int, _c.c_uint32, _c.c_uint64, _c.c_int, _c.c_uint64,
+                                       _c.c_int, _c.c_uint64, _c.POINTER(_c.c_float), _c.c_int]),
+    "omr_ntt_planner_set": (_c.c_int, [_c.c_int, _c.c_uint32, _c.c_uint64, _c.c_int, _c.c_uint64,
+                                        _c.c_int, _c.c_int]),
+    "omr_ntt_planner_get": (_c.c_int, [_c.c_int, _c.c_uint32, _c.c_uint64, _c.c_int, _c.c_uint64,
+                                        _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
+    "omr_ntt_planner_clear": (_c.c_int, []),
+    "omr_ntt_planner_save": (_c.c_int, [_c.c_char_p]),
+    "omr_ntt_planner_load": (_c.c_int, [_c.c_char_p]),
     "omr_ntt_last_error": (_c.c_char_p, []),
     "omr_ntt_version": (_c.c_char_p, []),
 }
