@@ -15,9 +15,10 @@ namespace omr {
 // adds its outputs k over the group's columns into registers.  A second
 // kernel sums the per-CTA rows.  The input is read once; m words are written.
 template <class F, int LOGT>
-constexpr int prefix_cols() {
-  constexpr int c = 4096 >> LOGT;
-  return c < 8 ? 8 : (c > 256 ? 256 : c);
+constexpr int prefix_cols() {  // >= one 32-byte sector per row, tile <= 64 KiB (<= 128 KiB at T = 4096)
+  constexpr int lo = 32 / F::WORD;
+  constexpr int c = (65536 / F::WORD) >> LOGT;
+  return c < lo ? lo : (c > 256 ? 256 : c);
 }
 template <class F, int LOGT>
 constexpr int prefix_threads() {
