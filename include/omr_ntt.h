@@ -209,6 +209,44 @@ int omr_ntt_plan_passes(int field, uint32_t log_n, int plan, uint64_t batch, uin
 int omr_ntt_plan_run_pass(omr_ntt_domain_t d, int plan, int pass, int inverse, const void *src,
                           void *scratch, void *dst, uint64_t batch, void *stream);
 
+/* ---------------------------------------------------------------- batches */
+
+/* A mixed batch: many requests of different sizes (2^10 <= N <= 2^20),
+ * fields (BabyBear, Goldilocks), directions and output sets, executed by one
+ * persistent kernel that drains a device-side queue of tile tasks, launched
+ * through a CUDA graph captured on the first run.  No reference counterpart
+ * (the reference runs one encoder call at a time). */
+typedef struct omr_ntt_batch_s *omr_ntt_batch_t;
+
+int omr_ntt_batch_create(omr_ntt_batch_t *out);
+int omr_ntt_batch_destroy(omr_ntt_batch_t b);
+
+/* Add one request.  Its N words of input sit at byte offset `in_offset` of
+ * the input arena, its output at `out_offset` of the output arena: N words for
+ * a full transform (pattern < 0, or count >= N), else `count` words selected
+ * by the host index set `host_indices` (pattern OMR_NTT_PATTERN_INDICES).
+ * Returns the request's index (>= 0) or a negative status. */
+int omr_ntt_batch_add(omr_ntt_batch_t b, int field, uint32_t log_n, int inverse, int pattern,
+                      uint64_t count, const uint32_t *host_indices, uint64_t in_offset,
+                      uint64_t out_offset);
+
+/* Freeze the batch: plan every request, order the tile tasks, upload the
+ * queue, allocate the scratch arena. */
+int omr_ntt_batch_build(omr_ntt_batch_t b);
+int omr_ntt_batch_info(omr_ntt_batch_t b, uint64_t *requests, uint64_t *tasks,
+                       uint64_t *scratch_bytes);
+
+/* Run the whole batch: one graph launch (counter reset + persistent kernel).
+ * The graph is re-captured when the arena pointers change. */
+int omr_ntt_batch_run(omr_ntt_batch_t b, const void *in, void *out, void *stream);
+
+/* Synchronise and report a bounded dependency wait that gave up. */
+int omr_ntt_batch_check(omr_ntt_batch_t b, void *stream);
+
+/* Baseline: the same requests through the plain kernels, one request after
+ * another (what a caller of omr_ntt_forward / omr_ntt_inverse would do). */
+int omr_ntt_batch_run_per_request(omr_ntt_batch_t b, const void *in, void *out, void *stream);
+
 /* ---------------------------------------------------------------- planner */
 
 /* Candidate plans of a planning point (field, log2 N, output pattern, count;

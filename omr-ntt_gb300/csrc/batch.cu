@@ -1,0 +1,560 @@
+// batch.cu -- mixed batches of NTT requests in one persistent kernel.
+//
+// A batch holds requests of different sizes (2^10 .. 2^20 points), fields
+// (BabyBear, Goldilocks), directions and output sets (full, or a partial
+// output at given indices).  The host builder splits every request into tile
+// tasks of the engine's two-pass four-step plan and orders them by phase:
+//   phase 0  column pass of every request  (input arena -> scratch A)
+//   phase 1  row pass of every request     (scratch A -> output, or scratch B)
+//   phase 2  gathers of partial requests   (scratch B -> output)
+// One persistent kernel drains that device-side queue: each CTA claims the
+// next task with an atomic ticket, waits (bounded, acquire) until the
+// request's previous phase is complete, runs the tile, and publishes its
+// completion (fence + atomic add).  Tasks only ever wait on tasks claimed
+// before them, so the queue cannot deadlock; every wait is bounded and raises
+// the batch's error word (OMR_NTT_ERR_TIMEOUT) instead of hanging.  The
+// counter reset and the kernel are captured once in a CUDA graph and replayed
+// per run.
+//
+// Inverse requests use the forward plan and the identity
+// INTT(X)[i] = N^-1 NTT(X)[(N - i) mod N]: the row pass stores index K at
+// (N - K) mod N scaled by N^-1, so one set of kernels serves both directions.
+//
+// The per-request baseline (omr_ntt_batch_run_per_request) launches the
+// plain kernels request by request, as a caller of the ordinary entry points
+// would.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "engine.cuh"
+#include "partial.cuh"
+
+namespace omr {
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchMinLog = 10, kBatchMaxLog = 20;
+constexpr int kGatherChunk = 1024;
+
+struct BatchReq {
+  int field, log_n, t1, t2, inverse, partial;
+  uint32_t count;
+  uint64_t in_off, out_off, scr_a, scr_b, idx_off;  // byte offsets (idx_off: uint32 index)
+  const void* tw_lo;                                 // forward four-step tables of (field, log_n)
+  const void* tw_hi;
+  uint64_t n_inv;                                    // N^-1 (canonical)
+  uint32_t groups0, groups1, groups2;
+};
+
+struct BatchTask {
+  uint32_t req;
+  uint32_t phase;  // 0, 1, 2
+  uint32_t group;
+};
+
+struct BatchArgs {
+  const BatchReq* reqs;
+  const BatchTask* tasks;
+  uint32_t ntasks;
+  unsigned int* next;   // ticket counter
+  unsigned int* done;   // [nreq][3] completed tasks per phase
+  int* err;
+  const char* in;
+  char* out;
+  char* scratch;
+  const uint32_t* idx;
+  const void* roots_bb;  // omega_4096 tables (forward)
+  const void* roots_gl;
+};
+
+template <class F>
+constexpr int batch_cols(int logt) {
+  int c = 2048 >> logt;
+  if (c > 64) c = 64;
+  return c < 32 / F::WORD ? 32 / F::WORD : c;
+}
+
+OMR_D unsigned int ld_acquire(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <class F, int LOGT, int C, int I>
+OMR_D void batch_col_rounds(const PassArgs<F>& a, typename F::E* s, const typename F::E* gin,
+                            typename F::E* gout, int nvalid, uint32_t llo0) {
+  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  if constexpr (I < RP::ROUNDS) {
+    constexpr bool first = I == 0, last = I + 1 == RP::ROUNDS;
+    do_round<F, LOGT, C, kBatchThreads, RP::logr(I), RP::logns(I), false,
+             first ? SRC_GLOBAL : SRC_SMEM, last ? DST_GLOBAL : DST_SMEM, false, true>(
+        a, s, gin, gout, nvalid, llo0, 0);
+    batch_col_rounds<F, LOGT, C, I + 1>(a, s, gin, gout, nvalid, llo0);
+  }
+}
+
+template <class F, int LOGT, int C, int I>
+OMR_D void batch_row_rounds(const PassArgs<F>& a, typename F::E* s, int nvalid, uint32_t llo0) {
+  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  if constexpr (I < RP::ROUNDS) {
+    constexpr bool last = I + 1 == RP::ROUNDS;
+    do_round<F, LOGT, C, kBatchThreads, RP::logr(I), RP::logns(I), false, SRC_SMEM,
+             last ? DST_STAGE : DST_SMEM, false, false>(a, s, nullptr, nullptr, nvalid, llo0, 0);
+    batch_row_rounds<F, LOGT, C, I + 1>(a, s, nvalid, llo0);
+  }
+}
+
+// Column pass tile (phase 0): T = 2^t1 rows, lines = N2 columns.
+template <class F, int LOGT>
+OMR_D void batch_col_tile(const BatchArgs& ba, const BatchReq& r, uint32_t g, typename F::E* s) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int C = batch_cols<F>(LOGT);
+  const uint32_t n2 = 1u << r.t2;
+  PassArgs<F> a{};
+  a.L_lo = n2;
+  a.es_in = n2;
+  a.es_out = n2;
+  a.roots = static_cast<const Tw*>(F::ID == BABYBEAR ? ba.roots_bb : ba.roots_gl);
+  a.roots_stride = 1u << (kMaxLogT - LOGT);
+  a.tw_lo = static_cast<const E*>(r.tw_lo);
+  a.tw_hi = static_cast<const Tw*>(r.tw_hi);
+  a.tw_scale = 1;
+  a.tw_mask = (1u << r.log_n) - 1;
+  a.tw_line_mul_m = 0;
+  a.has_scale = 0;
+  const uint32_t llo0 = g * C;
+  const int nvalid = (int)min((uint32_t)C, n2 - llo0);
+  const E* gin = reinterpret_cast<const E*>(ba.in + r.in_off) + llo0;
+  E* gout = reinterpret_cast<E*>(ba.scratch + r.scr_a) + llo0;
+  batch_col_rounds<F, LOGT, C, 0>(a, s, gin, gout, nvalid, llo0);
+}
+
+// Row pass tile (phase 1): T = 2^t2 points per line, lines = N1 rows; output
+// index K = k1 + N1 k2 (reversed and scaled for inverse requests).
+template <class F, int LOGT>
+OMR_D void batch_row_tile(const BatchArgs& ba, const BatchReq& r, uint32_t g, typename F::E* s) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int T = 1 << LOGT;
+  constexpr int C = batch_cols<F>(LOGT);
+  constexpr int TC = T * C;
+  const uint32_t n1 = 1u << r.t1, n = 1u << r.log_n;
+  const uint32_t llo0 = g * C;
+  const int nvalid = (int)min((uint32_t)C, n1 - llo0);
+  const E* src = reinterpret_cast<const E*>(ba.scratch + r.scr_a) + (uint64_t)llo0 * T;
+  // stage rows (t-fast, L2-coherent loads: written by other CTAs in phase 0)
+  for (int i = threadIdx.x; i < TC; i += kBatchThreads) {
+    const int t = i % T, c = i / T;
+    s[tile_idx<F, C>(t, c)] = c < nvalid ? __ldcg(src + (uint32_t)c * T + t) : (E)0;
+  }
+  __syncthreads();
+  PassArgs<F> a{};
+  a.roots = static_cast<const Tw*>(F::ID == BABYBEAR ? ba.roots_bb : ba.roots_gl);
+  a.roots_stride = 1u << (kMaxLogT - LOGT);
+  batch_row_rounds<F, LOGT, C, 0>(a, s, nvalid, llo0);
+  E* dst = reinterpret_cast<E*>(r.partial ? ba.scratch + r.scr_b : ba.out + r.out_off);
+  const typename F::Tw scale = F::make_tw(r.n_inv);
+  for (int i = threadIdx.x; i < TC; i += kBatchThreads) {
+    const int c = i % C, k = i / C;
+    if (c >= nvalid) continue;
+    E y = s[tile_idx<F, C>(k, c)];
+    uint32_t K = llo0 + c + (uint32_t)k * n1;
+    if (r.inverse) {
+      K = (n - K) & (n - 1);
+      y = F::mul_tw(y, scale);
+    }
+    dst[K] = y;
+  }
+}
+
+template <class F>
+OMR_D void batch_gather(const BatchArgs& ba, const BatchReq& r, uint32_t g) {
+  using E = typename F::E;
+  const E* full = reinterpret_cast<const E*>(ba.scratch + r.scr_b);
+  E* dst = reinterpret_cast<E*>(ba.out + r.out_off);
+  const uint32_t* idx = ba.idx + r.idx_off;
+  const uint32_t n = 1u << r.log_n;
+  for (uint32_t j = g * kGatherChunk + threadIdx.x; j < min(r.count, (g + 1) * kGatherChunk);
+       j += kBatchThreads)
+    dst[j] = __ldcg(full + (idx[j] & (n - 1)));
+}
+
+template <class F>
+OMR_D void batch_dispatch(const BatchArgs& ba, const BatchReq& r, const BatchTask& t, void* smem) {
+  using E = typename F::E;
+  E* s = reinterpret_cast<E*>(smem);
+  if (t.phase == 2) {
+    batch_gather<F>(ba, r, t.group);
+    return;
+  }
+  const int lt = t.phase == 0 ? r.t1 : r.t2;
+#define OMR_BATCH_CASE(L)                                   \
+  case L:                                                   \
+    if (t.phase == 0)                                       \
+      batch_col_tile<F, L>(ba, r, t.group, s);              \
+    else                                                    \
+      batch_row_tile<F, L>(ba, r, t.group, s);              \
+    break;
+  switch (lt) {
+    OMR_BATCH_CASE(5)
+    OMR_BATCH_CASE(6)
+    OMR_BATCH_CASE(7)
+    OMR_BATCH_CASE(8)
+    OMR_BATCH_CASE(9)
+    OMR_BATCH_CASE(10)
+    default: break;
+  }
+#undef OMR_BATCH_CASE
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(const BatchArgs ba) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ uint32_t task_id;
+  __shared__ int abort_flag;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      task_id = atomicAdd(ba.next, 1u);
+      abort_flag = 0;
+      if (task_id < ba.ntasks) {
+        const BatchTask t = ba.tasks[task_id];
+        if (t.phase > 0) {
+          const BatchReq& r = ba.reqs[t.req];
+          const unsigned int need = t.phase == 1 ? r.groups0 : r.groups1;
+          const unsigned int* ctr = ba.done + 3 * t.req + (t.phase - 1);
+          bool ok = false;
+          for (unsigned long long i = 0; i < (1ull << 26); i++) {
+            if (ld_acquire(ctr) >= need) {
+              ok = true;
+              break;
+            }
+            __nanosleep(64);
+          }
+          if (!ok) {
+            atomicExch(ba.err, OMR_NTT_ERR_TIMEOUT);
+            abort_flag = 1;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const uint32_t tid = task_id;
+    if (tid >= ba.ntasks) break;
+    if (abort_flag) {
+      // the dependency never completed: skip the task but still publish it so
+      // that no later task waits forever on this one
+    } else {
+      const BatchTask t = ba.tasks[tid];
+      const BatchReq r = ba.reqs[t.req];
+      if (r.field == BABYBEAR)
+        batch_dispatch<BabyBear>(ba, r, t, smem_raw);
+      else
+        batch_dispatch<Goldilocks>(ba, r, t, smem_raw);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const BatchTask t = ba.tasks[tid];
+      __threadfence();
+      atomicAdd(ba.done + 3 * t.req + t.phase, 1u);
+    }
+  }
+}
+
+constexpr size_t kBatchSmem = 32 * 1024;
+
+}  // namespace omr
+
+using namespace omr;
+
+struct omr_ntt_batch_s {
+  int device = 0;
+  std::vector<BatchReq> reqs;
+  std::vector<uint32_t> idx;  // concatenated partial index sets
+  std::vector<uint64_t> idx_count;
+  std::map<std::pair<int, int>, omr_ntt_domain_t> domains;
+  std::vector<BatchTask> tasks;
+  bool built = false;
+  // device state
+  BatchReq* d_reqs = nullptr;
+  BatchTask* d_tasks = nullptr;
+  uint32_t* d_idx = nullptr;
+  unsigned int* d_ctr = nullptr;  // [0] ticket, [1..] done counters
+  int* d_err = nullptr;
+  char* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  size_t ctr_bytes = 0;
+  // graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* g_in = nullptr;
+  void* g_out = nullptr;
+  int grid = 0;
+};
+
+static int batch_domain(omr_ntt_batch_s* b, int field, int log_n, omr_ntt_domain_t* out) {
+  auto key = std::make_pair(field, log_n);
+  auto it = b->domains.find(key);
+  if (it != b->domains.end()) {
+    *out = it->second;
+    return OMR_NTT_OK;
+  }
+  omr_ntt_domain_t d = nullptr;
+  int rc = omr_ntt_domain_create(field, (uint32_t)log_n, &d);
+  if (rc) return rc;
+  b->domains[key] = d;
+  *out = d;
+  return OMR_NTT_OK;
+}
+
+static void batch_free_device(omr_ntt_batch_s* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  cudaFree(b->d_reqs);
+  cudaFree(b->d_tasks);
+  cudaFree(b->d_idx);
+  cudaFree(b->d_ctr);
+  cudaFree(b->d_err);
+  cudaFree(b->d_scratch);
+  b->d_reqs = nullptr;
+  b->d_tasks = nullptr;
+  b->d_idx = nullptr;
+  b->d_ctr = nullptr;
+  b->d_err = nullptr;
+  b->d_scratch = nullptr;
+}
+
+static BatchArgs batch_args(omr_ntt_batch_s* b, const void* in, void* out) {
+  RootTables bb, gl;
+  get_root_tables(BABYBEAR, &bb);
+  get_root_tables(GOLDILOCKS, &gl);
+  BatchArgs a{};
+  a.reqs = b->d_reqs;
+  a.tasks = b->d_tasks;
+  a.ntasks = (uint32_t)b->tasks.size();
+  a.next = b->d_ctr;
+  a.done = b->d_ctr + 1;
+  a.err = b->d_err;
+  a.in = static_cast<const char*>(in);
+  a.out = static_cast<char*>(out);
+  a.scratch = b->d_scratch;
+  a.idx = b->d_idx;
+  a.roots_bb = bb.fwd;
+  a.roots_gl = gl.fwd;
+  return a;
+}
+
+extern "C" {
+
+int omr_ntt_batch_create(omr_ntt_batch_t* out) {
+  if (!out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null output handle");
+  auto* b = new (std::nothrow) omr_ntt_batch_s();
+  if (!b) return fail(OMR_NTT_ERR_ALLOC, "batch allocation failed");
+  cudaGetDevice(&b->device);
+  *out = b;
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_batch_destroy(omr_ntt_batch_t b) {
+  if (!b) return OMR_NTT_OK;
+  DeviceGuard g(b->device);
+  cudaDeviceSynchronize();
+  batch_free_device(b);
+  for (auto& kv : b->domains) omr_ntt_domain_destroy(kv.second);
+  delete b;
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_batch_add(omr_ntt_batch_t b, int field, uint32_t log_n, int inverse, int pattern,
+                      uint64_t count, const uint32_t* host_indices, uint64_t in_offset,
+                      uint64_t out_offset) {
+  if (!b) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null batch");
+  if (b->built) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "batch already built");
+  if (field != BABYBEAR && field != GOLDILOCKS)
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "batch requests are BabyBear or Goldilocks");
+  if ((int)log_n < kBatchMinLog || (int)log_n > kBatchMaxLog)
+    return fail(OMR_NTT_ERR_SIZE, "batch requests need 2^10 <= N <= 2^20");
+  const uint64_t n = 1ull << log_n;
+  const bool partial = pattern >= 0 && count < n;
+  if (partial && (pattern != OMR_NTT_PATTERN_INDICES || !host_indices || count == 0))
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "partial batch requests give an index set");
+  const size_t w = word_bytes(field);
+  if ((in_offset % w) || (out_offset % w))
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "offsets must be multiples of the word size");
+  if (partial)
+    for (uint64_t j = 0; j < count; j++)
+      if (host_indices[j] >= n) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "index out of range");
+  BatchReq r{};
+  r.field = field;
+  r.log_n = (int)log_n;
+  r.t1 = (int)(log_n + 1) / 2;
+  r.t2 = (int)log_n / 2;
+  r.inverse = inverse ? 1 : 0;
+  r.partial = partial ? 1 : 0;
+  r.count = partial ? (uint32_t)count : (uint32_t)n;
+  r.in_off = in_offset;
+  r.out_off = out_offset;
+  r.idx_off = b->idx.size();
+  if (partial) b->idx.insert(b->idx.end(), host_indices, host_indices + count);
+  b->reqs.push_back(r);
+  return (int)b->reqs.size() - 1;
+}
+
+int omr_ntt_batch_build(omr_ntt_batch_t b) {
+  if (!b) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null batch");
+  if (b->built) return OMR_NTT_OK;
+  if (b->reqs.empty()) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "empty batch");
+  DeviceGuard g(b->device);
+  size_t scr = 0;
+  for (auto& r : b->reqs) {
+    omr_ntt_domain_t d = nullptr;
+    int rc = batch_domain(b, r.field, r.log_n, &d);
+    if (rc) return rc;
+    const size_t w = word_bytes(r.field);
+    const uint64_t n = 1ull << r.log_n;
+    r.tw_lo = d->tw_lo_f;
+    r.tw_hi = d->tw_hi_f;
+    r.n_inv = d->n_inv;
+    scr = (scr + 255) / 256 * 256;
+    r.scr_a = scr;
+    scr += n * w;
+    scr = (scr + 255) / 256 * 256;
+    r.scr_b = scr;
+    if (r.partial) scr += n * w;
+    const int c1 = r.field == BABYBEAR ? batch_cols<BabyBear>(r.t1) : batch_cols<Goldilocks>(r.t1);
+    const int c2 = r.field == BABYBEAR ? batch_cols<BabyBear>(r.t2) : batch_cols<Goldilocks>(r.t2);
+    r.groups0 = (uint32_t)(((1ull << r.t2) + c1 - 1) / c1);
+    r.groups1 = (uint32_t)(((1ull << r.t1) + c2 - 1) / c2);
+    r.groups2 = r.partial ? (r.count + kGatherChunk - 1) / kGatherChunk : 0;
+  }
+  // tasks ordered by phase: a task only waits on tasks claimed before it
+  b->tasks.clear();
+  for (uint32_t ph = 0; ph < 3; ph++)
+    for (uint32_t i = 0; i < b->reqs.size(); i++) {
+      const BatchReq& r = b->reqs[i];
+      const uint32_t ng = ph == 0 ? r.groups0 : (ph == 1 ? r.groups1 : r.groups2);
+      for (uint32_t gi = 0; gi < ng; gi++) b->tasks.push_back(BatchTask{i, ph, gi});
+    }
+  b->scratch_bytes = scr;
+  b->ctr_bytes = sizeof(unsigned int) * (1 + 3 * b->reqs.size());
+  cudaError_t e = cudaSuccess;
+  if ((e = cudaMalloc(&b->d_reqs, sizeof(BatchReq) * b->reqs.size())) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_tasks, sizeof(BatchTask) * b->tasks.size())) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_idx, sizeof(uint32_t) * std::max<size_t>(1, b->idx.size()))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_ctr, b->ctr_bytes)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_err, sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_scratch, std::max<size_t>(256, scr))) != cudaSuccess) {
+    batch_free_device(b);
+    return fail(OMR_NTT_ERR_ALLOC, std::string("batch device state: ") + cudaGetErrorString(e));
+  }
+  OMR_CUDA_TRY(cudaMemcpy(b->d_reqs, b->reqs.data(), sizeof(BatchReq) * b->reqs.size(),
+                          cudaMemcpyHostToDevice));
+  OMR_CUDA_TRY(cudaMemcpy(b->d_tasks, b->tasks.data(), sizeof(BatchTask) * b->tasks.size(),
+                          cudaMemcpyHostToDevice));
+  if (!b->idx.empty())
+    OMR_CUDA_TRY(cudaMemcpy(b->d_idx, b->idx.data(), sizeof(uint32_t) * b->idx.size(),
+                            cudaMemcpyHostToDevice));
+  OMR_CUDA_TRY(cudaMemset(b->d_err, 0, sizeof(int)));
+  OMR_CUDA_TRY(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kBatchSmem));
+  int occ = 0;
+  OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kBatchThreads,
+                                                             kBatchSmem));
+  b->grid = device_sm_count(b->device) * (occ < 1 ? 1 : occ);
+  b->built = true;
+  return OMR_NTT_OK;
+}
+
+// Total scratch bytes the batch owns and the number of queued tile tasks.
+int omr_ntt_batch_info(omr_ntt_batch_t b, uint64_t* requests, uint64_t* tasks,
+                       uint64_t* scratch_bytes) {
+  if (!b) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null batch");
+  if (requests) *requests = b->reqs.size();
+  if (tasks) *tasks = b->tasks.size();
+  if (scratch_bytes) *scratch_bytes = b->scratch_bytes;
+  return OMR_NTT_OK;
+}
+
+int omr_ntt_batch_run(omr_ntt_batch_t b, const void* in, void* out, void* stream) {
+  if (!b || !in || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!b->built) {
+    int rc = omr_ntt_batch_build(b);
+    if (rc) return rc;
+  }
+  DeviceGuard g(b->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!b->exec || b->g_in != in || b->g_out != out) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    cudaStream_t cap = nullptr;
+    OMR_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    const BatchArgs a = batch_args(b, in, out);
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      cudaMemsetAsync(b->d_ctr, 0, b->ctr_bytes, cap);
+      batch_kernel<<<b->grid, kBatchThreads, kBatchSmem, cap>>>(a);
+      e = cudaStreamEndCapture(cap, &b->graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return fail(OMR_NTT_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    b->g_in = in;
+    b->g_out = out;
+  }
+  OMR_CUDA_TRY(cudaGraphLaunch(b->exec, st));
+  return OMR_NTT_OK;
+}
+
+// Error word of the batch (OMR_NTT_ERR_TIMEOUT if a bounded wait gave up);
+// synchronises `stream` and clears the word.
+int omr_ntt_batch_check(omr_ntt_batch_t b, void* stream) {
+  if (!b || !b->built) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "batch not built");
+  DeviceGuard g(b->device);
+  int h = 0;
+  OMR_CUDA_TRY(cudaMemcpyAsync(&h, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  OMR_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  if (h) {
+    cudaMemset(b->d_err, 0, sizeof(int));
+    return fail(h, "a batch task's bounded dependency wait gave up");
+  }
+  return OMR_NTT_OK;
+}
+
+// Baseline: the same requests through the plain per-request kernels.
+int omr_ntt_batch_run_per_request(omr_ntt_batch_t b, const void* in, void* out, void* stream) {
+  if (!b || !in || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  if (!b->built) {
+    int rc = omr_ntt_batch_build(b);
+    if (rc) return rc;
+  }
+  DeviceGuard g(b->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  for (auto& r : b->reqs) {
+    omr_ntt_domain_t d = b->domains[std::make_pair(r.field, r.log_n)];
+    const char* x = static_cast<const char*>(in) + r.in_off;
+    char* y = static_cast<char*>(out) + r.out_off;
+    int rc;
+    if (!r.partial) {
+      rc = run_transform(d, -1, r.inverse != 0, x, y, 1, st);
+    } else {
+      char* full = b->d_scratch + r.scr_b;
+      rc = run_transform(d, -1, r.inverse != 0, x, full, 1, st);
+      if (!rc)
+        rc = with_field(r.field, [&](auto f) -> int {
+          using F = decltype(f);
+          return launch_gather_indices<F>(full, d->n, r.count, b->d_idx + r.idx_off, y, st);
+        });
+    }
+    if (rc) return rc;
+  }
+  return OMR_NTT_OK;
+}
+
+}  // extern "C"

@@ -304,6 +304,21 @@ int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uin
   return run_gather<F>(d, -1, pattern, count, indices, in, out, stream);
 }
 
+template <class F>
+int launch_gather_indices(const void* full, uint64_t n, uint64_t count, const uint32_t* idx,
+                          void* out, cudaStream_t stream) {
+  using E = typename F::E;
+  if (count == 0) return OMR_NTT_OK;
+  gather_kernel<F><<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(
+      static_cast<const E*>(full), n, OMR_NTT_PATTERN_INDICES, count, idx, static_cast<E*>(out));
+  OMR_CUDA_TRY(cudaGetLastError());
+  return OMR_NTT_OK;
+}
+template int launch_gather_indices<BabyBear>(const void*, uint64_t, uint64_t, const uint32_t*,
+                                             void*, cudaStream_t);
+template int launch_gather_indices<Goldilocks>(const void*, uint64_t, uint64_t, const uint32_t*,
+                                               void*, cudaStream_t);
+
 template int partial_dispatch<BabyBear>(omr_ntt_domain_s*, int, uint64_t, const uint32_t*,
                                         const void*, void*, cudaStream_t);
 template int partial_dispatch<Goldilocks>(omr_ntt_domain_s*, int, uint64_t, const uint32_t*,

@@ -29,6 +29,11 @@ int run_partial_strategy(omr_ntt_domain_s* d, int strategy, int param, int patte
                          uint64_t count, const uint32_t* indices, const void* in, void* out,
                          cudaStream_t stream);
 
+// out[j] = full[idx[j]] (j < count) on `stream`.
+template <class F>
+int launch_gather_indices(const void* full, uint64_t n, uint64_t count, const uint32_t* idx,
+                          void* out, cudaStream_t stream);
+
 template <class F>
 int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uint32_t* indices,
                      const void* in, void* out, cudaStream_t stream);

@@ -82,6 +82,16 @@ _SIGS = {
     "omr_ntt_planner_clear": (_c.c_int, []),
     "omr_ntt_planner_save": (_c.c_int, [_c.c_char_p]),
     "omr_ntt_planner_load": (_c.c_int, [_c.c_char_p]),
+    "omr_ntt_batch_create": (_c.c_int, [_c.POINTER(_c.c_void_p)]),
+    "omr_ntt_batch_destroy": (_c.c_int, [_c.c_void_p]),
+    "omr_ntt_batch_add": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_uint32, _c.c_int, _c.c_int,
+                                      _c.c_uint64, _c.c_void_p, _c.c_uint64, _c.c_uint64]),
+    "omr_ntt_batch_build": (_c.c_int, [_c.c_void_p]),
+    "omr_ntt_batch_info": (_c.c_int, [_c.c_void_p, _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
+                                       _c.POINTER(_c.c_uint64)]),
+    "omr_ntt_batch_run": (_c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_void_p]),
+    "omr_ntt_batch_check": (_c.c_int, [_c.c_void_p, _c.c_void_p]),
+    "omr_ntt_batch_run_per_request": (_c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_void_p]),
     "omr_ntt_last_error": (_c.c_char_p, []),
     "omr_ntt_version": (_c.c_char_p, []),
 }

@@ -1,0 +1,91 @@
+"""Mixed batches in one persistent, graph-launched kernel: every request's
+output is bit-exact against the oracle (small batch) and against the
+per-request plain kernels (the full 4096-request mixed workload)."""
+import numpy as np
+import pytest
+
+from omr_ntt import OmrNttError
+from omr_ntt.batch import Batch, Request, fill_inputs, layout, mixed_requests
+from omr_ntt.fields import BabyBear, Goldilocks
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_inputs(nbytes, seed):
+    """Canonical words for both fields: 32-bit lanes below 2^30."""
+    import torch
+
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    lanes = torch.randint(0, 1 << 30, ((nbytes + 3) // 4,), dtype=torch.int32, device="cuda", generator=g)
+    return lanes.view(torch.uint8)[:nbytes]
+
+
+def _run(reqs, seed, per_request=False, device_inputs=False):
+    import torch
+
+    ib, ob = layout(reqs)
+    if device_inputs:
+        host_in = None
+        d_in = _device_inputs(ib, seed)
+    else:
+        host_in = fill_inputs(reqs, ib, seed)
+        d_in = torch.from_numpy(host_in).cuda()
+    d_out = torch.zeros(max(ob, 1), dtype=torch.uint8, device="cuda")
+    b = Batch(reqs)
+    if per_request:
+        b.run_per_request(d_in.data_ptr(), d_out.data_ptr())
+    else:
+        b.run(d_in.data_ptr(), d_out.data_ptr())
+    b.check()
+    torch.cuda.synchronize()
+    return host_in, d_out.cpu().numpy(), b
+
+
+def test_small_mixed_batch_against_oracle(oracle):
+    reqs = mixed_requests(7, count=48, min_log=10, max_log=15)
+    host_in, out, b = _run(reqs, 3)
+    for i, r in enumerate(reqs):
+        w = r.field.word_bytes
+        x = host_in[r.in_off:r.in_off + r.n * w].view(r.field.dtype)
+        full = oracle.inverse(r.field.id, x) if r.inverse else oracle.forward(r.field.id, x)
+        exp = full if r.indices is None else full[r.indices.astype(np.int64)]
+        got = out[r.out_off:r.out_off + r.out_words * w].view(r.field.dtype)
+        assert np.array_equal(got, exp), (i, r.field, r.log_n, r.inverse, r.indices is not None)
+
+
+def test_graph_replay_and_rerun(oracle):
+    import torch
+
+    reqs = [Request(BabyBear, 12, False), Request(Goldilocks, 11, True),
+            Request(BabyBear, 20, True, np.array([0, 5, 77, (1 << 20) - 1], dtype=np.uint32))]
+    ib, ob = layout(reqs)
+    host_in = fill_inputs(reqs, ib, 11)
+    d_in = torch.from_numpy(host_in).cuda()
+    d_out = torch.zeros(ob, dtype=torch.uint8, device="cuda")
+    b = Batch(reqs)
+    for _ in range(3):  # replays of the captured graph give the same words
+        d_out.zero_()
+        b.run(d_in.data_ptr(), d_out.data_ptr())
+        b.check()
+        out = d_out.cpu().numpy()
+        r = reqs[2]
+        x = host_in[r.in_off:r.in_off + r.n * 4].view(np.uint32)
+        exp = oracle.inverse(0, x)[r.indices.astype(np.int64)]
+        assert np.array_equal(out[r.out_off:r.out_off + 16].view(np.uint32), exp)
+
+
+def test_full_mixed_workload_matches_per_request():
+    reqs = mixed_requests(2024, count=4096)
+    _, out_batch, b = _run(reqs, 5, device_inputs=True)
+    info = b.info()
+    assert info["requests"] == 4096 and info["tasks"] > 4096
+    del b
+    _, out_plain, _ = _run(reqs, 5, per_request=True, device_inputs=True)
+    assert np.array_equal(out_batch, out_plain)
+
+
+def test_batch_rejects_out_of_range_sizes():
+    with pytest.raises(OmrNttError):
+        Batch([Request(BabyBear, 22, False)])
+    with pytest.raises(OmrNttError):
+        Batch([Request(BabyBear, 12, False, np.array([1 << 12], dtype=np.uint32))])
