@@ -318,6 +318,10 @@ template int launch_gather_indices<BabyBear>(const void*, uint64_t, uint64_t, co
                                              void*, cudaStream_t);
 template int launch_gather_indices<Goldilocks>(const void*, uint64_t, uint64_t, const uint32_t*,
                                                void*, cudaStream_t);
+template int launch_gather_indices<KoalaBear>(const void*, uint64_t, uint64_t, const uint32_t*,
+                                              void*, cudaStream_t);
+template int launch_gather_indices<TeddyBear>(const void*, uint64_t, uint64_t, const uint32_t*,
+                                              void*, cudaStream_t);
 
 template int partial_dispatch<BabyBear>(omr_ntt_domain_s*, int, uint64_t, const uint32_t*,
                                         const void*, void*, cudaStream_t);
