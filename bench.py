@@ -304,6 +304,66 @@ def main():
                 "GB/s_alg": round(gbs, 1), "frac_hbm": round(gbs / peak, 3)}
             del t, dd
 
+    # ---- partial outputs (n = 2^22, s = 2^4..2^16, three index patterns)
+    partial = {}
+    if not args.no_extras:
+        import omr_ntt.inputs as oin
+
+        for fld in (BabyBear, Goldilocks):
+            nn = 1 << 22
+            dd = NttDomain(fld, nn)
+            t = torch.empty(nn, dtype=torch.int32 if fld.word_bytes == 4 else torch.int64, device="cuda")
+            t.random_(0, 1 << 30)
+            row = {}
+            for k in range(4, 17, 2):
+                sc = 1 << k
+                o = torch.empty(sc, dtype=t.dtype, device="cuda")
+                idx = torch.from_numpy(oin.random_indices(nn, sc, k).view(np.int32)).cuda()
+                for pat, nm in ((0, "prefix"), (1, "strided"), (2, "random")):
+                    ip = ctypes.c_void_p(idx.data_ptr()) if pat == 2 else None
+                    ms = timed(lambda: _lib.check(L.omr_ntt_partial(dd.handle, pat, sc, ip, ctypes.c_void_p(t.data_ptr()),
+                                                                    ctypes.c_void_p(o.data_ptr()), sp)), reps=5)
+                    row[f"s=2^{k} {nm}"] = round(ms, 4)
+            partial[fld.name] = row
+            del t, dd
+
+    # ---- mixed batch: one graph-launched persistent kernel vs per-request kernels
+    mixed = None
+    if not args.no_extras:
+        from omr_ntt.batch import Batch, layout, mixed_requests
+
+        reqs = mixed_requests(2024, count=4096)
+        ib, ob = layout(reqs)
+        g = torch.Generator(device="cuda").manual_seed(5)
+        d_in = torch.randint(0, 1 << 30, ((ib + 3) // 4,), dtype=torch.int32, device="cuda", generator=g)
+        d_out = torch.empty(ob, dtype=torch.uint8, device="cuda")
+        bt = Batch(reqs)
+        bt.run(d_in.data_ptr(), d_out.data_ptr(), stream.cuda_stream)  # capture + warm-up
+        bt.run_per_request(d_in.data_ptr(), d_out.data_ptr(), stream.cuda_stream)
+        torch.cuda.synchronize()
+
+        def tmix(fn, reps=5):
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ts.sort()
+            return ts[len(ts) // 2]
+
+        ms_b = tmix(lambda: bt.run(d_in.data_ptr(), d_out.data_ptr(), stream.cuda_stream))
+        ms_p = tmix(lambda: bt.run_per_request(d_in.data_ptr(), d_out.data_ptr(), stream.cuda_stream))
+        bt.check(stream.cuda_stream)
+        elems = sum(r.n for r in reqs)
+        mixed = {"requests": len(reqs), "elements": elems, "tasks": bt.info()["tasks"],
+                 "graph_persistent_ms": round(ms_b, 3), "per_request_ms": round(ms_p, 3),
+                 "speedup": round(ms_p / ms_b, 2), "graph_Gelem/s": round(elems / ms_b / 1e6, 2)}
+        bt.close()
+        del d_in, d_out
+
     # ---- CPU baseline (rank 0, N=1 only): the oracle port on the host cores
     cpu = None
     if rank == 0 and world == 1:
@@ -337,6 +397,8 @@ def main():
             "gpu_launches": len(passes) * args.steps,
             "clocks": clocks,
             "extras": extras,
+            "partial_ms": partial,
+            "mixed_batch": mixed,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
