@@ -283,6 +283,40 @@ int omr_ntt_planner_clear(void);
 int omr_ntt_planner_save(const char *path);
 int omr_ntt_planner_load(const char *path);
 
+/* ---------------------------------------------------------------- learned planner */
+
+/* Plan classes: a fixed vocabulary of 40 plans independent of N (12 full
+ * transform pass-split x kernel classes, 4 prefix decomposition line lengths,
+ * 12 strided-fold sub-plan classes, 12 full-then-gather classes).
+ * omr_ntt_plan_class_candidate maps class `cls` of a planning point to its
+ * concrete candidate (returns 1) or reports it not applicable (0). */
+int omr_ntt_plan_class_count(void);
+int omr_ntt_plan_class_candidate(int field, uint32_t log_n, int pattern, uint64_t count, int cls,
+                                 int *strategy, int *param);
+int omr_ntt_planner_use_mlp(int enable);
+
+/* The learned selector: an fp32 MLP (n_in -> n_hidden -> n_hidden -> n_out,
+ * ReLU) trained on the GPU by the library's own forward, backward and Adam
+ * kernels on the autotuner's timings.  Input: the 10 features of
+ * omr_ntt_mlp_features; output: one predicted (centred) log time per plan
+ * class.  Installed with omr_ntt_mlp_install, the planner (plan = -1, partial
+ * entry points) takes the applicable class with the lowest prediction when
+ * its database has no entry.  No reference counterpart. */
+typedef struct omr_ntt_mlp_s *omr_ntt_mlp_t;
+int omr_ntt_mlp_features(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                         float *features10);
+int omr_ntt_mlp_create(int n_in, int n_hidden, int n_out, uint64_t seed, omr_ntt_mlp_t *out);
+int omr_ntt_mlp_destroy(omr_ntt_mlp_t m);
+int omr_ntt_mlp_param_count(omr_ntt_mlp_t m);
+int omr_ntt_mlp_get_params(omr_ntt_mlp_t m, float *host);
+int omr_ntt_mlp_set_params(omr_ntt_mlp_t m, const float *host);
+int omr_ntt_mlp_forward(omr_ntt_mlp_t m, const float *x, int batch, float *y);
+int omr_ntt_mlp_gradients(omr_ntt_mlp_t m, const float *x, const float *target, const float *mask,
+                          int batch, float *grad, float *loss);
+int omr_ntt_mlp_fit(omr_ntt_mlp_t m, const float *x, const float *target, const float *mask, int n,
+                    int epochs, int batch, float lr, uint64_t seed, float *loss_history);
+int omr_ntt_mlp_install(omr_ntt_mlp_t m);
+
 /* ---------------------------------------------------------------- misc */
 
 const char *omr_ntt_last_error(void);

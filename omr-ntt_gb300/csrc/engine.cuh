@@ -55,8 +55,12 @@ struct PlanShape {
 std::vector<PlanShape> enumerate_plans(uint32_t log_n);
 std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanShape& shape);
 int default_plan(int field, uint32_t log_n, uint64_t batch);
-// The planner's full-transform plan: planner database, else built-in heuristic (tuner.cu).
+// The planner's full-transform plan: planner database, learned selector, else
+// built-in heuristic (tuner.cu).
 int planned_full_plan(int field, uint32_t log_n, uint64_t batch);
+// The planner's partial strategy (1 if the database or the learned selector has one).
+int planned_partial(int field, uint32_t log_n, int pattern, uint64_t count, int* strategy,
+                    int* param);
 
 // ------------------------------------------------------------------ device tables
 // Per-field in-line roots omega_4096^k, k < 4096 (forward and inverse),

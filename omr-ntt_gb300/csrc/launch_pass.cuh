@@ -112,16 +112,17 @@ int launch_tma_k(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   constexpr size_t smem = tma_smem_total<F, LOGT, C, NBUF>();
   static_assert(smem <= kMaxDynSmem, "TMA pass tile does not fit in shared memory");
   auto kern = ntt_tile_pass_tma<F, LOGT, C, NT, MODE, INV, TW, NBUF>;
-  static std::atomic<size_t> attr_bytes[64];
+  // per device: attribute set and occupancy queried once (both cost host time)
+  static std::atomic<int> occ_cache[64];
   int dev = 0;
   cudaGetDevice(&dev);
-  if (attr_bytes[dev & 63].load() < smem) {
+  int occ = occ_cache[dev & 63].load();
+  if (occ == 0) {
     OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem));
-    attr_bytes[dev & 63] = kMaxDynSmem;
+    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
+    if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "TMA pass does not fit on an SM");
+    occ_cache[dev & 63] = occ;
   }
-  int occ = 0;
-  OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
-  if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "TMA pass does not fit on an SM");
   const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
   if (ntiles == 0) return OMR_NTT_OK;
   CUtensorMap in_map, out_map;

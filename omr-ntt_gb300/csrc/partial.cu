@@ -1,6 +1,8 @@
 // partial.cu -- partial-output transform kernels (see partial.cuh).
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "partial.cuh"
 
 namespace omr {
@@ -47,12 +49,15 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>())
   constexpr int T = 1 << LOGT;
   constexpr int C = prefix_cols<F, LOGT>();
   constexpr int NT = prefix_threads<F, LOGT>();
-  constexpr int KPER = (T + NT - 1) / NT;
+  // thread -> (output k, slice of the group's columns): TPK threads per output
+  constexpr int TPK = NT > T ? NT / T : 1;
+  constexpr int KPER = TPK > 1 ? 1 : T / NT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E* s = reinterpret_cast<E*>(smem_raw);
   E acc[KPER];
 #pragma unroll
   for (int i = 0; i < KPER; i++) acc[i] = 0;
+  const int slice = TPK > 1 ? (int)threadIdx.x / T : 0;
   const uint32_t groups = (a.L_lo + C - 1) / C;
   for (uint32_t g = blockIdx.x; g < groups; g += gridDim.x) {
     const uint32_t llo0 = g * C;
@@ -60,20 +65,29 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>())
     prefix_rounds<F, LOGT, C, NT, 0>(a, s, a.in + llo0, nvalid, llo0);
 #pragma unroll
     for (int i = 0; i < KPER; i++) {
-      const int k = threadIdx.x + i * NT;
-      if (k < (int)m) {
-        E sum = acc[i];
-#pragma unroll 8
-        for (int c = 0; c < C; c++) sum = F::add(sum, s[tile_idx<F, C>(k, c)]);
-        acc[i] = sum;
-      }
+      const int k = TPK > 1 ? (int)threadIdx.x % T : (int)threadIdx.x + i * NT;
+      E sum = acc[i];
+#pragma unroll 4
+      for (int c = slice; c < C; c += TPK) sum = F::add(sum, s[tile_idx<F, C>(k, c)]);
+      acc[i] = sum;
     }
     __syncthreads();  // the next group's first round overwrites the tile
   }
+  if constexpr (TPK > 1) {
+    // combine the TPK slices of every output in shared memory
+    s[threadIdx.x] = acc[0];
+    __syncthreads();
+    if ((int)threadIdx.x < T && threadIdx.x < m) {
+      E sum = 0;
+      for (int sl = 0; sl < TPK; sl++) sum = F::add(sum, s[sl * T + threadIdx.x]);
+      partial[(uint64_t)blockIdx.x * m + threadIdx.x] = sum;
+    }
+  } else {
 #pragma unroll
-  for (int i = 0; i < KPER; i++) {
-    const int k = threadIdx.x + i * NT;
-    if (k < (int)m) partial[(uint64_t)blockIdx.x * m + k] = acc[i];
+    for (int i = 0; i < KPER; i++) {
+      const int k = threadIdx.x + i * NT;
+      if (k < (int)m) partial[(uint64_t)blockIdx.x * m + k] = acc[i];
+    }
   }
 }
 
@@ -98,8 +112,17 @@ static int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void
   constexpr int NT = prefix_threads<F, LOGT>();
   constexpr size_t smem = (size_t)T * C * sizeof(E);
   auto kern = prefix_decomp_kernel<F, LOGT>;
-  if (smem > 48 * 1024)
-    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static std::atomic<int> occ_cache[64];
+  int dev = 0;
+  OMR_CUDA_TRY(cudaGetDevice(&dev));
+  int occ = occ_cache[dev & 63].load();
+  if (occ == 0) {
+    if (smem > 48 * 1024)
+      OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
+    occ_cache[dev & 63] = occ < 1 ? 1 : occ;
+    occ = occ_cache[dev & 63];
+  }
   RootTables rt;
   int rc = get_root_tables(F::ID, &rt);
   if (rc) return rc;
@@ -117,12 +140,8 @@ static int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void
   a.tw_scale = 1;
   a.tw_mask = (uint32_t)(d->n - 1);
   a.tw_line_mul_m = 0;
-  int occ = 0;
-  OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
-  int dev = 0;
-  OMR_CUDA_TRY(cudaGetDevice(&dev));
   const uint32_t groups = (a.L_lo + C - 1) / C;
-  uint32_t grid = (uint32_t)device_sm_count(dev) * (uint32_t)(occ < 1 ? 1 : occ);
+  uint32_t grid = (uint32_t)device_sm_count(dev) * (uint32_t)occ;
   if (grid > groups) grid = groups;
   void* part = nullptr;
   rc = domain_scratch(d, stream, (size_t)grid * m * sizeof(E), &part, 1);
@@ -214,6 +233,33 @@ static int launch_colsum(const typename F::E* x, uint64_t rows, uint64_t cols,
 
 enum { STRAT_DECOMP_ = 1, STRAT_FOLD_ = 2, STRAT_GATHER_ = 3 };
 
+// Strided fold for narrow outputs (count <= 4096): one grid-stride sweep over
+// x with a stride that is a multiple of count, so every thread stays in one
+// column; per-CTA partial column sums land in partial[rows][count].
+template <class F>
+__global__ void __launch_bounds__(256) fold_flat_kernel(const typename F::E* __restrict__ x,
+                                                        uint64_t n, uint32_t count,
+                                                        typename F::E* __restrict__ partial) {
+  using E = typename F::E;
+  __shared__ E red[256];
+  const uint64_t stride = (uint64_t)gridDim.x * 256;
+  E acc = 0;
+  for (uint64_t i = blockIdx.x * 256ull + threadIdx.x; i < n; i += stride) acc = F::add(acc, x[i]);
+  if (count >= 256) {
+    // this CTA covers 256 distinct columns; replica row = blockIdx / (count / 256)
+    const uint32_t per = count / 256;
+    partial[(uint64_t)(blockIdx.x / per) * count + (blockIdx.x % per) * 256 + threadIdx.x] = acc;
+    return;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x < count) {
+    E sum = 0;
+    for (uint32_t j = threadIdx.x; j < 256; j += count) sum = F::add(sum, red[j]);
+    partial[(uint64_t)blockIdx.x * count + threadIdx.x] = sum;
+  }
+}
+
 template <class F>
 static int run_fold(omr_ntt_domain_s* d, int sub_plan, uint64_t count, const void* in, void* out,
                     cudaStream_t stream) {
@@ -232,8 +278,15 @@ static int run_fold(omr_ntt_domain_s* d, int sub_plan, uint64_t count, const voi
   if (rc) return rc;
   E* part = static_cast<E*>(buf);
   uint64_t nch = 0;
-  rc = launch_colsum<F>(static_cast<const E*>(in), rows, count, part, max_chunks, &nch, stream);
-  if (rc) return rc;
+  if (count <= 4096 && d->n >= 256ull * 1216) {
+    const uint32_t grid = 1216;  // 8 CTAs per SM; a multiple of count / 256 for count <= 4096
+    fold_flat_kernel<F><<<grid, 256, 0, stream>>>(static_cast<const E*>(in), d->n, (uint32_t)count, part);
+    OMR_CUDA_TRY(cudaGetLastError());
+    nch = count >= 256 ? grid / (count / 256) : grid;
+  } else {
+    rc = launch_colsum<F>(static_cast<const E*>(in), rows, count, part, max_chunks, &nch, stream);
+    if (rc) return rc;
+  }
   E* y = part;
   if (nch > 1) {
     y = part + nch * count;
@@ -294,7 +347,7 @@ int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uin
                      const void* in, void* out, cudaStream_t stream) {
   const uint64_t n = d->n;
   int strategy = 0, param = 0;
-  if (omr_ntt_planner_get(d->field, d->log_n, 1, pattern, count, &strategy, &param) == 1 &&
+  if (planned_partial(d->field, d->log_n, pattern, count, &strategy, &param) == 1 &&
       strategy >= STRAT_DECOMP_ && strategy <= STRAT_GATHER_)
     return run_strategy_t<F>(d, strategy, param, pattern, count, indices, in, out, stream);
   if (pattern == OMR_NTT_PATTERN_STRIDED && count < n)

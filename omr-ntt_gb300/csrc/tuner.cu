@@ -61,6 +61,99 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
   return v;
 }
 
+// ------------------------------------------------------------------ plan classes
+// A fixed, size-independent plan vocabulary for the learned planner:
+//   0..11   full transform: (pass-count offset 0/1, balanced/reversed split) x kernel variant 0..2
+//   12..15  prefix decomposition with line length next_pow2(count) << j, j = 0..3
+//   16..27  strided fold, then the count-point transform with full class (c - 16)
+//   28..39  full transform with full class (c - 28), then gather
+constexpr int kNumClasses = 40;
+
+// plan id of full class fc (0..11) for a 2^log_n transform, or -1
+static int full_class_plan(uint32_t log_n, int fc) {
+  const auto plans = enumerate_plans(log_n);
+  if (log_n == 0) return fc == 0 ? 0 : -1;
+  const int variant = fc / 4, po = (fc % 4) / 2, rev = fc % 2;
+  const int pmin = std::max<int>(1, (int)((log_n + kMaxLogT - 1) / kMaxLogT));
+  const int P = pmin + po;
+  if ((uint32_t)P > log_n || P > 3) return -1;
+  std::vector<int> bal(P);
+  for (int i = 0; i < P; i++) bal[i] = (int)(log_n / P) + (i < (int)(log_n % P) ? 1 : 0);
+  if (bal[0] > kMaxLogT) return -1;
+  std::vector<int> want = bal;
+  if (rev) {
+    std::reverse(want.begin(), want.end());
+    if (want == bal) return -1;  // same as the balanced class
+  }
+  if (P == 1 && variant > 0) return -1;  // single-pass plans have one kernel
+  for (int i = 0; i < (int)plans.size(); i++)
+    if (plans[i].split == want && plans[i].variant == variant) return i;
+  return -1;
+}
+
+static bool class_candidate(int field, uint32_t log_n, int pattern, uint64_t count, int cls,
+                            Cand* out) {
+  (void)field;
+  const uint64_t n = 1ull << log_n;
+  const bool full = count >= n || count == 0;
+  if (cls < 0 || cls >= kNumClasses) return false;
+  if (cls < 12) {
+    if (!full) return false;
+    int p = full_class_plan(log_n, cls);
+    if (p < 0) return false;
+    *out = Cand{STRAT_FULL, p};
+    return true;
+  }
+  if (full) return false;
+  if (cls < 16) {
+    if (pattern != OMR_NTT_PATTERN_PREFIX || count > 4096) return false;
+    int lt = 0;
+    while ((1ull << lt) < count) lt++;
+    if (lt == 0) lt = 1;
+    lt += cls - 12;
+    if (lt > kMaxLogT || (uint32_t)lt >= log_n) return false;
+    *out = Cand{STRAT_DECOMP, lt};
+    return true;
+  }
+  if (cls < 28) {
+    if (pattern != OMR_NTT_PATTERN_STRIDED || (count & (count - 1))) return false;
+    uint32_t ls = 0;
+    while ((1ull << ls) < count) ls++;
+    int p = full_class_plan(ls, cls - 16);
+    if (p < 0) return false;
+    *out = Cand{STRAT_FOLD, p};
+    return true;
+  }
+  int p = full_class_plan(log_n, cls - 28);
+  if (p < 0) return false;
+  *out = Cand{STRAT_GATHER, p};
+  return true;
+}
+
+// The learned selector installed in the planner (mlp.cu); returns the class
+// with the lowest predicted cost among the applicable ones, or -1.
+int mlp_select_class(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                     const bool* applicable, int n_classes);
+
+static bool g_use_mlp = false;
+
+static bool mlp_choice(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                       Cand* out) {
+  if (!g_use_mlp) return false;
+  bool app[kNumClasses];
+  Cand cands[kNumClasses];
+  bool any = false;
+  for (int c = 0; c < kNumClasses; c++) {
+    app[c] = class_candidate(field, log_n, pattern, count, c, &cands[c]);
+    any |= app[c];
+  }
+  if (!any) return false;
+  int c = mlp_select_class(field, log_n, batch, pattern, count, app, kNumClasses);
+  if (c < 0 || !app[c]) return false;
+  *out = cands[c];
+  return true;
+}
+
 // ------------------------------------------------------------------ planner DB
 struct Key {
   int field, log_n, batch_log, pattern, count_log;
@@ -113,7 +206,22 @@ int planned_full_plan(int field, uint32_t log_n, uint64_t batch) {
   const int n = (int)enumerate_plans(log_n).size();
   if (db_lookup(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
     return c.param;
+  if (mlp_choice(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
+    return c.param;
   return heuristic_full_plan(field, log_n, batch);
+}
+
+// Planner choice for a partial request: database, learned selector, else 0
+// (the caller's built-in heuristic).
+int planned_partial(int field, uint32_t log_n, int pattern, uint64_t count, int* strategy,
+                    int* param) {
+  Cand c;
+  if (db_lookup(field, log_n, 1, pattern, count, &c) || mlp_choice(field, log_n, 1, pattern, count, &c)) {
+    *strategy = c.strategy;
+    *param = c.param;
+    return 1;
+  }
+  return 0;
 }
 
 // ------------------------------------------------------------------ executors
@@ -210,6 +318,25 @@ int omr_ntt_planner_load(const char* path) {
     }
   }
   return n;
+}
+
+// Plan classes ---------------------------------------------------------------
+
+int omr_ntt_plan_class_count(void) { return kNumClasses; }
+
+int omr_ntt_plan_class_candidate(int field, uint32_t log_n, int pattern, uint64_t count, int cls,
+                                 int* strategy, int* param) {
+  if (!valid_field(field) || (int)log_n > two_adicity(field)) return 0;
+  Cand c;
+  if (!class_candidate(field, log_n, pattern, count, cls, &c)) return 0;
+  if (strategy) *strategy = c.strategy;
+  if (param) *param = c.param;
+  return 1;
+}
+
+int omr_ntt_planner_use_mlp(int enable) {
+  g_use_mlp = enable != 0;
+  return OMR_NTT_OK;
 }
 
 // Candidates -----------------------------------------------------------------

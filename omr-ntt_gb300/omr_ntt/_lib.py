@@ -92,6 +92,25 @@ _SIGS = {
     "omr_ntt_batch_run": (_c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_void_p]),
     "omr_ntt_batch_check": (_c.c_int, [_c.c_void_p, _c.c_void_p]),
     "omr_ntt_batch_run_per_request": (_c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_void_p]),
+    "omr_ntt_plan_class_count": (_c.c_int, []),
+    "omr_ntt_plan_class_candidate": (_c.c_int, [_c.c_int, _c.c_uint32, _c.c_int, _c.c_uint64, _c.c_int,
+                                                 _c.POINTER(_c.c_int), _c.POINTER(_c.c_int)]),
+    "omr_ntt_planner_use_mlp": (_c.c_int, [_c.c_int]),
+    "omr_ntt_mlp_features": (_c.c_int, [_c.c_int, _c.c_uint32, _c.c_uint64, _c.c_int, _c.c_uint64,
+                                         _c.POINTER(_c.c_float)]),
+    "omr_ntt_mlp_create": (_c.c_int, [_c.c_int, _c.c_int, _c.c_int, _c.c_uint64, _c.POINTER(_c.c_void_p)]),
+    "omr_ntt_mlp_destroy": (_c.c_int, [_c.c_void_p]),
+    "omr_ntt_mlp_param_count": (_c.c_int, [_c.c_void_p]),
+    "omr_ntt_mlp_get_params": (_c.c_int, [_c.c_void_p, _c.POINTER(_c.c_float)]),
+    "omr_ntt_mlp_set_params": (_c.c_int, [_c.c_void_p, _c.POINTER(_c.c_float)]),
+    "omr_ntt_mlp_forward": (_c.c_int, [_c.c_void_p, _c.POINTER(_c.c_float), _c.c_int, _c.POINTER(_c.c_float)]),
+    "omr_ntt_mlp_gradients": (_c.c_int, [_c.c_void_p, _c.POINTER(_c.c_float), _c.POINTER(_c.c_float),
+                                          _c.POINTER(_c.c_float), _c.c_int, _c.POINTER(_c.c_float),
+                                          _c.POINTER(_c.c_float)]),
+    "omr_ntt_mlp_fit": (_c.c_int, [_c.c_void_p, _c.POINTER(_c.c_float), _c.POINTER(_c.c_float),
+                                    _c.POINTER(_c.c_float), _c.c_int, _c.c_int, _c.c_int, _c.c_float,
+                                    _c.c_uint64, _c.POINTER(_c.c_float)]),
+    "omr_ntt_mlp_install": (_c.c_int, [_c.c_void_p]),
     "omr_ntt_last_error": (_c.c_char_p, []),
     "omr_ntt_version": (_c.c_char_p, []),
 }

@@ -1,0 +1,224 @@
+"""The learned plan selector: planning points, autotuner data, training, regret.
+
+A planning point is (field, log2 n, log2 s, output pattern, batch).  The
+exhaustive autotuner (omr_ntt_tune_point, native) times every candidate plan
+of the point; the 40 plan classes (omr_ntt_plan_class_candidate) give a fixed
+output vocabulary for the network.  The network (omr_ntt_mlp_*, trained on
+the GPU by the library's own kernels) predicts each applicable class's log
+time relative to the point's mean; its choice is the lowest prediction.
+Regret of a choice = time(choice) / time(exhaustive optimum) - 1.
+
+Points: field uniform in {BabyBear, Goldilocks}, log2 n uniform in [10, 24],
+log2 s uniform in [4, log2 n] (s = n is the full transform), pattern uniform in
+{contiguous, strided, random}, batch uniform in {1, 8, 64, 512}; points with
+batch * n > 2^26 words are drawn again (they would hold tens of GB per point).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import math
+import os
+
+import numpy as np
+
+from ._lib import check, lib
+from .fields import BabyBear, Goldilocks, field_by_id
+
+N_FEATURES = 10
+N_HIDDEN = 64
+PATTERNS = ("contiguous", "strided", "random")
+PATTERN_ID = {"contiguous": 0, "strided": 1, "random": 2}
+BATCHES = (1, 8, 64, 512)
+MAX_WORDS = 1 << 26
+
+
+def n_classes() -> int:
+    return lib().omr_ntt_plan_class_count()
+
+
+def planning_points(seed: int, count: int = 2000, min_log: int = 10, max_log: int = 24):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pts = []
+    while len(pts) < count:
+        field = BabyBear if rng.random() < 0.5 else Goldilocks
+        log_n = int(rng.integers(min_log, max_log + 1))
+        log_s = int(rng.integers(4, log_n + 1))
+        pattern = PATTERNS[int(rng.integers(0, 3))]
+        batch = BATCHES[int(rng.integers(0, 4))]
+        if batch << log_n > MAX_WORDS:
+            continue
+        pts.append({"field": field.id, "log_n": log_n, "log_s": log_s, "pattern": pattern,
+                    "batch": batch})
+    return pts
+
+
+def point_count(p) -> int:
+    return 1 << p["log_s"]
+
+
+def features(p) -> np.ndarray:
+    f = (ctypes.c_float * N_FEATURES)()
+    check_n = lib().omr_ntt_mlp_features(p["field"], p["log_n"], p["batch"], PATTERN_ID[p["pattern"]],
+                                         point_count(p), f)
+    assert check_n == N_FEATURES
+    return np.frombuffer(f, dtype=np.float32).copy()
+
+
+def candidates(p):
+    L = lib()
+    pat, cnt = PATTERN_ID[p["pattern"]], point_count(p)
+    n = L.omr_ntt_candidates(p["field"], p["log_n"], pat, cnt, None, None, 0)
+    st = (ctypes.c_int * n)()
+    pa = (ctypes.c_int * n)()
+    L.omr_ntt_candidates(p["field"], p["log_n"], pat, cnt, st, pa, n)
+    return list(zip(list(st), list(pa)))
+
+
+def class_map(p):
+    """class -> index into candidates(p) (or -1 when not applicable)."""
+    L = lib()
+    cands = candidates(p)
+    where = {c: i for i, c in enumerate(cands)}
+    out = []
+    s, q = ctypes.c_int(), ctypes.c_int()
+    for c in range(n_classes()):
+        ok = L.omr_ntt_plan_class_candidate(p["field"], p["log_n"], PATTERN_ID[p["pattern"]],
+                                            point_count(p), c, ctypes.byref(s), ctypes.byref(q))
+        out.append(where.get((s.value, q.value), -1) if ok else -1)
+    return out
+
+
+def tune(p, reps: int = 3, seed: int = 1):
+    """Exhaustive autotuner on the GPU: median ms of every candidate."""
+    cands = candidates(p)
+    ms = (ctypes.c_float * len(cands))()
+    rc = lib().omr_ntt_tune_point(p["field"], p["log_n"], p["batch"], PATTERN_ID[p["pattern"]],
+                                  point_count(p), reps, seed, ms, len(cands))
+    if rc < 0:
+        check(rc)
+    return np.array(list(ms), dtype=np.float64)
+
+
+def collect(points, reps: int = 3, progress=None):
+    """Dataset: features, class times (NaN: not applicable), exhaustive best."""
+    K = n_classes()
+    X = np.zeros((len(points), N_FEATURES), dtype=np.float32)
+    T = np.full((len(points), K), np.nan)
+    best = np.zeros(len(points))
+    for i, p in enumerate(points):
+        ms = tune(p, reps=reps, seed=1000 + i)
+        cm = class_map(p)
+        X[i] = features(p)
+        for c, j in enumerate(cm):
+            if j >= 0:
+                T[i, c] = ms[j]
+        best[i] = ms.min()
+        if progress and (i + 1) % progress == 0:
+            print(f"tuned {i + 1}/{len(points)}", flush=True)
+    return {"X": X, "T": T, "best": best}
+
+
+def targets(T):
+    """Centred log times and the mask of applicable classes."""
+    M = np.isfinite(T)
+    logt = np.where(M, np.log(np.where(M, T, 1.0)), 0.0)
+    mean = (logt * M).sum(1, keepdims=True) / np.maximum(M.sum(1, keepdims=True), 1)
+    Y = np.where(M, logt - mean, 0.0)
+    return Y.astype(np.float32), M.astype(np.float32)
+
+
+class Mlp:
+    """The library's MLP (device parameters, GPU training)."""
+
+    def __init__(self, seed: int = 0, n_out: int | None = None):
+        self.n_out = n_out or n_classes()
+        h = ctypes.c_void_p()
+        check(lib().omr_ntt_mlp_create(N_FEATURES, N_HIDDEN, self.n_out, seed, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def params(self) -> np.ndarray:
+        n = lib().omr_ntt_mlp_param_count(self._h)
+        buf = (ctypes.c_float * n)()
+        check(lib().omr_ntt_mlp_get_params(self._h, buf))
+        return np.frombuffer(buf, dtype=np.float32).copy()
+
+    def set_params(self, p):
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().omr_ntt_mlp_set_params(self._h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def forward(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        y = np.zeros((X.shape[0], self.n_out), dtype=np.float32)
+        check(lib().omr_ntt_mlp_forward(self._h, X.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                        X.shape[0], y.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return y
+
+    def gradients(self, X, Y, M):
+        X, Y, M = (np.ascontiguousarray(a, dtype=np.float32) for a in (X, Y, M))
+        g = np.zeros(lib().omr_ntt_mlp_param_count(self._h), dtype=np.float32)
+        loss = ctypes.c_float()
+        f = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        check(lib().omr_ntt_mlp_gradients(self._h, f(X), f(Y), f(M), X.shape[0], f(g), ctypes.byref(loss)))
+        return float(loss.value), g
+
+    def fit(self, X, Y, M, epochs=300, batch=64, lr=3e-3, seed=0):
+        X, Y, M = (np.ascontiguousarray(a, dtype=np.float32) for a in (X, Y, M))
+        hist = np.zeros(epochs, dtype=np.float32)
+        f = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        check(lib().omr_ntt_mlp_fit(self._h, f(X), f(Y), f(M), X.shape[0], epochs, batch, lr, seed, f(hist)))
+        return hist
+
+    def install(self):
+        check(lib().omr_ntt_mlp_install(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().omr_ntt_mlp_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def choose(pred, T):
+    """Index of the applicable class with the lowest prediction, per row."""
+    masked = np.where(np.isfinite(T), pred, np.inf)
+    return masked.argmin(1)
+
+
+def heuristic_class(p) -> int:
+    """The class the planner picks without database or network (its built-in
+    rule): tuned TMA kernel on the balanced split for the headline fields,
+    decomposition for prefixes <= 4096, fold for strided sets, else gather."""
+    full_cls = 4 if (p["log_n"] > 12 and p["field"] in (0, 1)) else 0
+    n, s = 1 << p["log_n"], point_count(p)
+    if s >= n:
+        return full_cls
+    if p["pattern"] == "strided":
+        sub_full = 4 if (p["log_s"] > 12 and p["field"] in (0, 1)) else 0
+        return 16 + sub_full
+    if p["pattern"] == "contiguous" and s <= 4096 and n // s >= 2:
+        return 12
+    return 28 + full_cls
+
+
+def regret(T, best, choice):
+    t = T[np.arange(len(choice)), choice]
+    return t / best - 1.0
+
+
+def save_model(path, mlp: Mlp, meta: dict):
+    np.savez(path, params=mlp.params(), meta=json.dumps(meta))
+
+
+def load_params(path):
+    z = np.load(path, allow_pickle=False)
+    return z["params"], json.loads(str(z["meta"]))
