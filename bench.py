@@ -183,6 +183,11 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
+    # the learned planner trained on GB300 picks every plan = -1 below
+    from omr_ntt import planner as lp
+
+    planner_file = lp.install_default()
+
     field = field_by_name(args.field)
     log_n = args.log_n
     n = 1 << log_n
@@ -364,6 +369,31 @@ def main():
         bt.close()
         del d_in, d_out
 
+    # ---- learned planner: stored held-out regret + a live re-tune of held-out points
+    learned = None
+    if not args.no_extras and rank == 0:
+        params, meta = lp.load_params(os.path.join(lp.DATA_DIR, "planner_mlp.npz"))
+        z = np.load(os.path.join(lp.DATA_DIR, "planner_dataset.npz"))
+        pts = json.loads(str(z["points"]))
+        net = lp.Mlp(seed=0)
+        net.set_params(params)
+        live = []
+        for p in pts[1500:1500 + 12]:
+            ms = lp.tune(p, reps=3, seed=7)
+            cm = lp.class_map(p)
+            pred = net.forward(lp.features(p)[None])[0]
+            app = [c for c, j in enumerate(cm) if j >= 0]
+            c = min(app, key=lambda c: pred[c])
+            live.append(float(ms[cm[c]] / ms.min() - 1.0))
+        net.close()
+        s = meta["summary"]
+        learned = {"held_out_points": s["held_out"], "classes": s["classes"],
+                   "regret_mean": s["regret_mlp"]["mean"], "regret_median": s["regret_mlp"]["median"],
+                   "regret_p90": s["regret_mlp"]["p90"], "within_5pct": s["regret_mlp"]["within_5pct"],
+                   "builtin_rule_regret_mean": s["regret_heuristic"]["mean"],
+                   "live_retune_points": len(live), "live_regret_mean": float(np.mean(live)),
+                   "network": os.path.relpath(planner_file, ROOT)}
+
     # ---- CPU baseline (rank 0, N=1 only): the oracle port on the host cores
     cpu = None
     if rank == 0 and world == 1:
@@ -399,6 +429,7 @@ def main():
             "extras": extras,
             "partial_ms": partial,
             "mixed_batch": mixed,
+            "learned_planner": learned,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

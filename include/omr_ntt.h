@@ -316,6 +316,9 @@ int omr_ntt_mlp_gradients(omr_ntt_mlp_t m, const float *x, const float *target, 
 int omr_ntt_mlp_fit(omr_ntt_mlp_t m, const float *x, const float *target, const float *mask, int n,
                     int epochs, int batch, float lr, uint64_t seed, float *loss_history);
 int omr_ntt_mlp_install(omr_ntt_mlp_t m);
+/* Load a network file ("OMRM", uint32 n_in, n_hidden, n_out, float32 params;
+ * omr-ntt_gb300/data/planner_mlp.bin is the network trained on GB300). */
+int omr_ntt_mlp_load(const char *path, omr_ntt_mlp_t *out);
 
 /* ---------------------------------------------------------------- misc */
 

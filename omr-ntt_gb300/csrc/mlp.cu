@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -359,6 +360,34 @@ int omr_ntt_mlp_fit(omr_ntt_mlp_t m, const float* x, const float* target, const 
     OMR_CUDA_TRY(cudaGetLastError());
     if (loss_hist) loss_hist[e] = (float)(tot / (nb ? nb : 1));
   }
+  return OMR_NTT_OK;
+}
+
+// Load a network written as: "OMRM", uint32 n_in, n_hidden, n_out, then the
+// float32 parameters (little endian, layout of omr_ntt_mlp_get_params).
+int omr_ntt_mlp_load(const char* path, omr_ntt_mlp_t* out) {
+  if (!path || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+  char magic[4];
+  uint32_t dims[3];
+  bool ok = std::fread(magic, 1, 4, f) == 4 && std::memcmp(magic, "OMRM", 4) == 0 &&
+            std::fread(dims, 4, 3, f) == 3 && dims[0] > 0 && dims[0] < 4096 && dims[1] > 0 &&
+            dims[1] < 4096 && dims[2] > 0 && dims[2] < 4096;
+  omr_ntt_mlp_t m = nullptr;
+  int rc = OMR_NTT_OK;
+  if (ok) rc = omr_ntt_mlp_create((int)dims[0], (int)dims[1], (int)dims[2], 0, &m);
+  if (ok && !rc) {
+    std::vector<float> p(m->nparam);
+    ok = std::fread(p.data(), sizeof(float), p.size(), f) == p.size();
+    if (ok) rc = omr_ntt_mlp_set_params(m, p.data());
+  }
+  std::fclose(f);
+  if (!ok || rc) {
+    omr_ntt_mlp_destroy(m);
+    return rc ? rc : fail(OMR_NTT_ERR_INVALID_ARGUMENT, std::string("malformed network file ") + path);
+  }
+  *out = m;
   return OMR_NTT_OK;
 }
 

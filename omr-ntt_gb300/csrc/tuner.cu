@@ -154,6 +154,17 @@ static bool mlp_choice(int field, uint32_t log_n, uint64_t batch, int pattern, u
   return true;
 }
 
+// Learned choice, remembered in the planner database so that later calls for
+// the same point skip the network.
+static void db_store(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                     const Cand& c);
+static bool mlp_choice_cached(int field, uint32_t log_n, uint64_t batch, int pattern,
+                              uint64_t count, Cand* out) {
+  if (!mlp_choice(field, log_n, batch, pattern, count, out)) return false;
+  db_store(field, log_n, batch, pattern, count, *out);
+  return true;
+}
+
 // ------------------------------------------------------------------ planner DB
 struct Key {
   int field, log_n, batch_log, pattern, count_log;
@@ -176,6 +187,12 @@ static Key make_key(int field, uint32_t log_n, uint64_t batch, int pattern, uint
   if (count >= n || count == 0) pattern = -1;  // full transform
   return Key{field, (int)log_n, ilog2_ceil(batch ? batch : 1), pattern,
              pattern < 0 ? (int)log_n : ilog2_ceil(count)};
+}
+
+static void db_store(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
+                     const Cand& c) {
+  std::lock_guard<std::mutex> lk(g_db_mu);
+  g_db[make_key(field, log_n, batch, pattern, count)] = c;
 }
 
 static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
@@ -206,7 +223,7 @@ int planned_full_plan(int field, uint32_t log_n, uint64_t batch) {
   const int n = (int)enumerate_plans(log_n).size();
   if (db_lookup(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
     return c.param;
-  if (mlp_choice(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
+  if (mlp_choice_cached(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
     return c.param;
   return heuristic_full_plan(field, log_n, batch);
 }
@@ -216,7 +233,8 @@ int planned_full_plan(int field, uint32_t log_n, uint64_t batch) {
 int planned_partial(int field, uint32_t log_n, int pattern, uint64_t count, int* strategy,
                     int* param) {
   Cand c;
-  if (db_lookup(field, log_n, 1, pattern, count, &c) || mlp_choice(field, log_n, 1, pattern, count, &c)) {
+  if (db_lookup(field, log_n, 1, pattern, count, &c) ||
+      mlp_choice_cached(field, log_n, 1, pattern, count, &c)) {
     *strategy = c.strategy;
     *param = c.param;
     return 1;

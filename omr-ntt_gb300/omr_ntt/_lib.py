@@ -111,6 +111,7 @@ _SIGS = {
                                     _c.POINTER(_c.c_float), _c.c_int, _c.c_int, _c.c_int, _c.c_float,
                                     _c.c_uint64, _c.POINTER(_c.c_float)]),
     "omr_ntt_mlp_install": (_c.c_int, [_c.c_void_p]),
+    "omr_ntt_mlp_load": (_c.c_int, [_c.c_char_p, _c.POINTER(_c.c_void_p)]),
     "omr_ntt_last_error": (_c.c_char_p, []),
     "omr_ntt_version": (_c.c_char_p, []),
 }

@@ -215,6 +215,33 @@ def regret(T, best, choice):
     return t / best - 1.0
 
 
+DATA_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "data")
+DEFAULT_NETWORK = os.path.join(DATA_DIR, "planner_mlp.bin")
+_default = None
+
+
+def install_default(path: str = DEFAULT_NETWORK):
+    """Load the network trained on GB300 and make it the planner's learned
+    selector (plan = -1 and the partial entry points then use it)."""
+    global _default
+    h = ctypes.c_void_p()
+    check(lib().omr_ntt_mlp_load(path.encode(), ctypes.byref(h)))
+    check(lib().omr_ntt_mlp_install(h))
+    if _default is not None:
+        lib().omr_ntt_mlp_destroy(_default)
+    _default = h
+    return path
+
+
+def uninstall():
+    global _default
+    lib().omr_ntt_mlp_install(None)
+    if _default is not None:
+        lib().omr_ntt_mlp_destroy(_default)
+        _default = None
+    lib().omr_ntt_planner_clear()
+
+
 def save_model(path, mlp: Mlp, meta: dict):
     np.savez(path, params=mlp.params(), meta=json.dumps(meta))
 
