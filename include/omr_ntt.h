@@ -243,6 +243,12 @@ int omr_ntt_batch_run(omr_ntt_batch_t b, const void *in, void *out, void *stream
 /* Synchronise and report a bounded dependency wait that gave up. */
 int omr_ntt_batch_check(omr_ntt_batch_t b, void *stream);
 
+/* Test-only fault injection (host side): request `req`'s row-pass tasks wait
+ * for one column tile more than exist, so their bounded waits (about a
+ * second) run out and omr_ntt_batch_check reports OMR_NTT_ERR_TIMEOUT; the
+ * CUDA context stays usable.  Use on a throw-away batch. */
+int omr_ntt_batch_inject_stall(omr_ntt_batch_t b, uint32_t req);
+
 /* Baseline: the same requests through the plain kernels, one request after
  * another (what a caller of omr_ntt_forward / omr_ntt_inverse would do). */
 int omr_ntt_batch_run_per_request(omr_ntt_batch_t b, const void *in, void *out, void *stream);

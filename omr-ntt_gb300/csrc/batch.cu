@@ -39,6 +39,8 @@ namespace omr {
 constexpr int kBatchThreads = 256;
 constexpr int kBatchMinLog = 10, kBatchMaxLog = 20;
 constexpr int kGatherChunk = 1024;
+// dependency waits give up after ~2^23 polls of >= 64 ns (about a second)
+constexpr unsigned long long kBatchSpinLimit = 1ull << 23;
 
 struct BatchReq {
   int field, log_n, t1, t2, inverse, partial;
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(const BatchArgs
           const unsigned int need = t.phase == 1 ? r.groups0 : r.groups1;
           const unsigned int* ctr = ba.done + 3 * t.req + (t.phase - 1);
           bool ok = false;
-          for (unsigned long long i = 0; i < (1ull << 26); i++) {
+          for (unsigned long long i = 0; i < kBatchSpinLimit; i++) {
             if (ld_acquire(ctr) >= need) {
               ok = true;
               break;
@@ -524,6 +526,20 @@ int omr_ntt_batch_check(omr_ntt_batch_t b, void* stream) {
     cudaMemset(b->d_err, 0, sizeof(int));
     return fail(h, "a batch task's bounded dependency wait gave up");
   }
+  return OMR_NTT_OK;
+}
+
+// Fault injection for tests (host side): request `req`'s row-pass tasks will
+// wait for one column tile more than exist, so their bounded waits run out
+// and the run reports OMR_NTT_ERR_TIMEOUT.  Undone by omr_ntt_batch_build of a
+// new batch only; use on a throw-away batch.
+int omr_ntt_batch_inject_stall(omr_ntt_batch_t b, uint32_t req) {
+  if (!b || !b->built || req >= b->reqs.size())
+    return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "bad batch or request");
+  DeviceGuard g(b->device);
+  BatchReq r = b->reqs[req];
+  r.groups0 += 1;
+  OMR_CUDA_TRY(cudaMemcpy(b->d_reqs + req, &r, sizeof(BatchReq), cudaMemcpyHostToDevice));
   return OMR_NTT_OK;
 }
 

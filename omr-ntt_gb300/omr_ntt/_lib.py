@@ -91,6 +91,7 @@ _SIGS = {
                                        _c.POINTER(_c.c_uint64)]),
     "omr_ntt_batch_run": (_c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_void_p]),
     "omr_ntt_batch_check": (_c.c_int, [_c.c_void_p, _c.c_void_p]),
+    "omr_ntt_batch_inject_stall": (_c.c_int, [_c.c_void_p, _c.c_uint32]),
     "omr_ntt_batch_run_per_request": (_c.c_int, [_c.c_void_p, _c.c_void_p, _c.c_void_p, _c.c_void_p]),
     "omr_ntt_plan_class_count": (_c.c_int, []),
     "omr_ntt_plan_class_candidate": (_c.c_int, [_c.c_int, _c.c_uint32, _c.c_int, _c.c_uint64, _c.c_int,

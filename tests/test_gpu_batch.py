@@ -89,3 +89,37 @@ def test_batch_rejects_out_of_range_sizes():
         Batch([Request(BabyBear, 22, False)])
     with pytest.raises(OmrNttError):
         Batch([Request(BabyBear, 12, False, np.array([1 << 12], dtype=np.uint32))])
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(oracle):
+    """A dependency that can never complete (host-side injection: a row pass
+    waiting for a column tile that does not exist) makes the persistent
+    kernel's bounded waits give up: the run reports OMR_NTT_ERR_TIMEOUT and
+    the next, correct run on the same context is bit-exact."""
+    import time
+
+    import torch
+    from omr_ntt import _lib
+
+    reqs = [Request(BabyBear, 12, False), Request(BabyBear, 14, False)]
+    ib, ob = layout(reqs)
+    host_in = fill_inputs(reqs, ib, 2)
+    d_in = torch.from_numpy(host_in).cuda()
+    d_out = torch.zeros(ob, dtype=torch.uint8, device="cuda")
+    bad = Batch(reqs)
+    assert _lib.lib().omr_ntt_batch_inject_stall(bad._h, 1) == 0
+    t0 = time.time()
+    bad.run(d_in.data_ptr(), d_out.data_ptr())
+    with pytest.raises(OmrNttError) as e:
+        bad.check()
+    assert e.value.status == -6  # OMR_NTT_ERR_TIMEOUT
+    assert time.time() - t0 < 60
+    bad.close()
+    good = Batch(reqs)
+    d_out.zero_()
+    good.run(d_in.data_ptr(), d_out.data_ptr())
+    good.check()
+    out = d_out.cpu().numpy()
+    for r in reqs:
+        x = host_in[r.in_off:r.in_off + r.n * 4].view(np.uint32)
+        assert np.array_equal(out[r.out_off:r.out_off + r.n * 4].view(np.uint32), oracle.forward(0, x))
