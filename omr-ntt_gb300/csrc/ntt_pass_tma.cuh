@@ -409,10 +409,13 @@ __global__ void __launch_bounds__(NT, 3 - NBUF)
   }
 }
 
-// Thread count of the TMA pass: EPT elements per thread.
+// Thread count of the TMA pass: EPT elements per thread.  16 keeps a
+// 32-bit-field thread at <= 64 registers, so a 4096-point tile runs as two
+// 512-thread CTAs per SM (NBUF = 1) whose barriers interleave; measured on
+// GB300 that beats 32 elements per thread (16 warps per SM) by ~11%.
 template <class F>
 constexpr int tma_ept() {
-  return F::WORD == 8 ? 16 : 32;
+  return 16;
 }
 template <class F, int LOGT, int NBUF>
 constexpr int tma_threads() {

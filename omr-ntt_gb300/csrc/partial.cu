@@ -9,97 +9,180 @@ namespace omr {
 
 // ---------------------------------------------------------------- prefix
 // Pruned prefix transform (the reference's TransformDecomposition,
-// src/encoders/transform_decomposition.rs:25-97, with n1 = T = next_pow2(m)):
-//   X[k] = sum_{r < N/T} omega_N^(r k) * DFT_T(x[r + (N/T) c] over c)[k],  k < m.
-// One persistent CTA walks groups of C adjacent columns r: T-point Stockham
-// rounds as in the tile pass (first round straight from global memory), the
-// last round leaves the twiddled outputs in shared memory, and each thread
-// adds its outputs k over the group's columns into registers.  A second
-// kernel sums the per-CTA rows.  The input is read once; m words are written.
+// src/encoders/transform_decomposition.rs:25-97, with n1 = T >= m):
+//   X[k] = sum_{r < N/T} omega_N^(r k) * Y_r[k],  Y_r = DFT_T(x[r + (N/T) c] over c),  k < m.
+// Each CTA owns a contiguous run of groups of C adjacent columns r.  Per group
+// it runs the T-point Stockham rounds of the tile pass (the first round reads
+// global memory straight into registers) into a shared-memory tile, then
+// folds the group into per-thread accumulators by Horner's rule over the
+// columns: thread (k, slice) visits columns r_i = r_first + slice + TPK i
+// (TPK column slices), acc = acc * omega_N^(-TPK k) + Y_{r_i}[k], and at the
+// end multiplies by omega_N^(k r_last); so sum_i omega_N^(k r_i) Y_{r_i}[k]
+// costs one constant multiply and one add per needed output and column,
+// with no per-element twiddle lookups.  The slices are combined in shared
+// memory, one row of m words per CTA, and a row-reduction kernel sums the
+// rows.  The input is read once.
 template <class F, int LOGT>
-constexpr int prefix_cols() {  // >= one 32-byte sector per row, tile <= 64 KiB (<= 128 KiB at T = 4096)
-  constexpr int lo = 32 / F::WORD;
+constexpr int prefix_cols() {  // ~64 KiB tile, rows of >= 16 bytes, <= 256 columns
+  constexpr int lo = 16 / F::WORD;
   constexpr int c = (65536 / F::WORD) >> LOGT;
   return c < lo ? lo : (c > 256 ? 256 : c);
 }
 template <class F, int LOGT>
-constexpr int prefix_threads() {
+constexpr int prefix_threads() {  // <= 256 threads at <= 128 registers: two CTAs per SM
   constexpr int tc = (1 << LOGT) * prefix_cols<F, LOGT>();
-  constexpr int nt = tc / (F::WORD == 8 ? 16 : 32);
-  return nt < 64 ? 64 : (nt > 512 ? 512 : nt);
+  constexpr int nt = tc / tile_ept<F>();
+  return nt < 64 ? 64 : (nt > 256 ? 256 : nt);
 }
 
 template <class F, int LOGT, int C, int NT, int I>
 OMR_D void prefix_rounds(const PassArgs<F>& a, typename F::E* s, const typename F::E* gin,
-                         int nvalid, uint32_t llo0) {
+                         int nvalid) {
   using RP = RoundPlan<LOGT, max_radix_log<F>()>;
   if constexpr (I < RP::ROUNDS) {
     constexpr int SRC = I == 0 ? SRC_GLOBAL : SRC_SMEM;
-    constexpr int DST = I + 1 == RP::ROUNDS ? DST_STAGE : DST_SMEM;
-    do_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), false, SRC, DST, false, true>(
-        a, s, gin, nullptr, nvalid, llo0, 0);
-    prefix_rounds<F, LOGT, C, NT, I + 1>(a, s, gin, nvalid, llo0);
+    do_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), false, SRC, DST_SMEM, false, false>(
+        a, s, gin, nullptr, nvalid, 0, 0);
+    prefix_rounds<F, LOGT, C, NT, I + 1>(a, s, gin, nvalid);
+  }
+}
+
+// omega_N^e in "twiddle-Montgomery" form (what mul_m takes) from the
+// two-level four-step tables.
+template <class F>
+OMR_D typename F::E omega_m(const PassArgs<F>& a, uint64_t e) {
+  const uint32_t ee = (uint32_t)e & a.tw_mask;
+  return F::mul_tw(a.tw_lo[ee & ((1u << kTwLoBits) - 1)], a.tw_hi[ee >> kTwLoBits]);
+}
+// omega_N^e as a twiddle operand for mul_tw.
+template <class F>
+OMR_D typename F::Tw omega_tw(const PassArgs<F>& a, uint64_t e) {
+  const typename F::E wm = omega_m<F>(a, e);
+  if constexpr (F::ID == GOLDILOCKS) {
+    return F::make_tw(wm);
+  } else {
+    return F::make_tw(F::mont(wm, 1u));  // canonical omega^e
   }
 }
 
 template <class F, int LOGT>
-__global__ void __launch_bounds__(prefix_threads<F, LOGT>())
+__global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
     prefix_decomp_kernel(const PassArgs<F> a, uint32_t m, typename F::E* __restrict__ partial) {
   using E = typename F::E;
+  using Tw = typename F::Tw;
   constexpr int T = 1 << LOGT;
   constexpr int C = prefix_cols<F, LOGT>();
   constexpr int NT = prefix_threads<F, LOGT>();
-  // thread -> (output k, slice of the group's columns): TPK threads per output
-  constexpr int TPK = NT > T ? NT / T : 1;
-  constexpr int KPER = TPK > 1 ? 1 : T / NT;
+  constexpr int KMAX = T > NT ? T / NT : 1;  // outputs per thread when m > NT
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E* s = reinterpret_cast<E*>(smem_raw);
-  E acc[KPER];
+
+  // thread -> KACT adjacent outputs x TPK column slices (m <= NT), or
+  // outputs k = t + j NT (m > NT, one slice)
+  uint32_t kact = 1;
+  while (kact < m && kact < (uint32_t)NT) kact <<= 1;
+  const uint32_t tpk = min((uint32_t)NT / kact, (uint32_t)C);
+  const uint32_t kper = (m + NT - 1) / NT;
+  const uint32_t kbase = threadIdx.x % kact;
+  const uint32_t slice = threadIdx.x / kact;
+  const bool active = slice < tpk;
+
+  E acc[KMAX];
+  Tw zi[KMAX];
 #pragma unroll
-  for (int i = 0; i < KPER; i++) acc[i] = 0;
-  const int slice = TPK > 1 ? (int)threadIdx.x / T : 0;
+  for (int j = 0; j < KMAX; j++) {
+    acc[j] = 0;
+    const uint32_t k = kbase + j * NT;
+    zi[j] = omega_tw<F>(a, (uint64_t)0 - (uint64_t)tpk * k);  // omega_N^(-TPK k)
+  }
+
   const uint32_t groups = (a.L_lo + C - 1) / C;
-  for (uint32_t g = blockIdx.x; g < groups; g += gridDim.x) {
+  const uint32_t g0 = (uint32_t)((uint64_t)blockIdx.x * groups / gridDim.x);
+  const uint32_t g1 = (uint32_t)((uint64_t)(blockIdx.x + 1) * groups / gridDim.x);
+  for (uint32_t g = g0; g < g1; g++) {
     const uint32_t llo0 = g * C;
     const int nvalid = (int)min((uint32_t)C, a.L_lo - llo0);
-    prefix_rounds<F, LOGT, C, NT, 0>(a, s, a.in + llo0, nvalid, llo0);
+    prefix_rounds<F, LOGT, C, NT, 0>(a, s, a.in + llo0, nvalid);
+    if (active) {
 #pragma unroll
-    for (int i = 0; i < KPER; i++) {
-      const int k = TPK > 1 ? (int)threadIdx.x % T : (int)threadIdx.x + i * NT;
-      E sum = acc[i];
+      for (int j = 0; j < KMAX; j++) {
+        const uint32_t k = kbase + j * NT;
+        if (j < (int)kper && k < m) {
+          E h = acc[j];
 #pragma unroll 4
-      for (int c = slice; c < C; c += TPK) sum = F::add(sum, s[tile_idx<F, C>(k, c)]);
-      acc[i] = sum;
+          for (uint32_t c = slice; c < (uint32_t)C; c += tpk)
+            h = F::add(F::mul_tw(h, zi[j]), s[tile_idx<F, C>((int)k, (int)c)]);
+          acc[j] = h;
+        }
+      }
     }
     __syncthreads();  // the next group's first round overwrites the tile
   }
-  if constexpr (TPK > 1) {
-    // combine the TPK slices of every output in shared memory
-    s[threadIdx.x] = acc[0];
+  if (g1 > g0) {
+    const uint64_t r_last = (uint64_t)(g1 - 1) * C + (C - tpk) + slice;
+#pragma unroll
+    for (int j = 0; j < KMAX; j++) {
+      const uint32_t k = kbase + j * NT;
+      if (active && j < (int)kper && k < m) acc[j] = mul_m<F>(acc[j], omega_m<F>(a, r_last * k));
+    }
+  }
+  if (tpk > 1) {
+    // combine the slices of every output: s[slice * kact + k]
+    if (active) s[slice * kact + kbase] = acc[0];
     __syncthreads();
-    if ((int)threadIdx.x < T && threadIdx.x < m) {
+    if (threadIdx.x < m) {
       E sum = 0;
-      for (int sl = 0; sl < TPK; sl++) sum = F::add(sum, s[sl * T + threadIdx.x]);
+      for (uint32_t sl = 0; sl < tpk; sl++) sum = F::add(sum, s[sl * kact + threadIdx.x]);
       partial[(uint64_t)blockIdx.x * m + threadIdx.x] = sum;
     }
   } else {
 #pragma unroll
-    for (int i = 0; i < KPER; i++) {
-      const int k = threadIdx.x + i * NT;
-      if (k < (int)m) partial[(uint64_t)blockIdx.x * m + k] = acc[i];
+    for (int j = 0; j < KMAX; j++) {
+      const uint32_t k = threadIdx.x + j * NT;
+      if (j < (int)kper && k < m) partial[(uint64_t)blockIdx.x * m + k] = acc[j];
     }
   }
 }
 
-// out[k] = sum over rows of partial[row * m + k]
+// out[k] = sum over rows of partial[row * cols + k].  A CTA of kReduceThreads
+// covers cw adjacent columns (cw a power of two <= 32) with kReduceThreads / cw
+// row slices, so each thread sums only rows / slices values (independent
+// loads, no long serial chain) before a shared-memory tree over the slices.
+constexpr int kReduceThreads = 1024;
+
 template <class F>
-__global__ void sum_rows_kernel(const typename F::E* __restrict__ partial, uint32_t rows, uint32_t m,
-                                typename F::E* __restrict__ out) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= m) return;
-  typename F::E acc = 0;
-  for (uint32_t r = 0; r < rows; r++) acc = F::add(acc, partial[(uint64_t)r * m + k]);
-  out[k] = acc;
+__global__ void __launch_bounds__(kReduceThreads)
+    reduce_rows_kernel(const typename F::E* __restrict__ partial, uint32_t rows, uint32_t cols,
+                       uint32_t cw, typename F::E* __restrict__ out) {
+  using E = typename F::E;
+  __shared__ E red[kReduceThreads];
+  const uint32_t slices = kReduceThreads / cw;
+  const uint32_t slice = threadIdx.x / cw;
+  const uint32_t c = blockIdx.x * cw + threadIdx.x % cw;
+  E acc = 0;
+  if (c < cols) {
+#pragma unroll 4
+    for (uint32_t r = slice; r < rows; r += slices) acc = F::add(acc, partial[(uint64_t)r * cols + c]);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (uint32_t h = slices >> 1; h >= 1; h >>= 1) {
+    if (slice < h) red[threadIdx.x] = F::add(red[threadIdx.x], red[threadIdx.x + h * cw]);
+    __syncthreads();
+  }
+  if (slice == 0 && c < cols) out[c] = red[threadIdx.x];
+}
+
+template <class F>
+static int launch_reduce_rows(const typename F::E* partial, uint64_t rows, uint64_t cols,
+                              typename F::E* out, cudaStream_t stream) {
+  uint32_t cw = 1;
+  while (cw < 32 && cw < cols) cw <<= 1;
+  const unsigned blocks = (unsigned)((cols + cw - 1) / cw);
+  reduce_rows_kernel<F><<<blocks, kReduceThreads, 0, stream>>>(partial, (uint32_t)rows, (uint32_t)cols,
+                                                               cw, out);
+  OMR_CUDA_TRY(cudaGetLastError());
+  return OMR_NTT_OK;
 }
 
 template <class F, int LOGT>
@@ -148,10 +231,7 @@ static int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void
   if (rc) return rc;
   kern<<<grid, NT, smem, stream>>>(a, m, static_cast<E*>(part));
   OMR_CUDA_TRY(cudaGetLastError());
-  sum_rows_kernel<F><<<(m + 255) / 256, 256, 0, stream>>>(static_cast<const E*>(part), grid, m,
-                                                           static_cast<E*>(out));
-  OMR_CUDA_TRY(cudaGetLastError());
-  return OMR_NTT_OK;
+  return launch_reduce_rows<F>(static_cast<const E*>(part), grid, m, static_cast<E*>(out), stream);
 }
 
 template <class F>
@@ -290,8 +370,7 @@ static int run_fold(omr_ntt_domain_s* d, int sub_plan, uint64_t count, const voi
   E* y = part;
   if (nch > 1) {
     y = part + nch * count;
-    uint64_t one = 0;
-    rc = launch_colsum<F>(part, nch, count, y, 1, &one, stream);
+    rc = launch_reduce_rows<F>(part, nch, count, y, stream);
     if (rc) return rc;
   }
   return run_transform(sd, sub_plan, false, y, out, 1, stream);

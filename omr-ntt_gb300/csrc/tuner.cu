@@ -214,7 +214,8 @@ static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   size_t nsplit = 0;
   for (auto& p : plans)
     if (p.variant == 0) nsplit++;
-  const int cand = (int)nsplit;  // variant 1, first (balanced) split
+  // BabyBear: variant 2 (two CTAs per SM); Goldilocks: variant 1 (double-buffered)
+  const int cand = (int)nsplit * (field == BABYBEAR ? 2 : 1);  // first (balanced) split
   return cand < (int)plans.size() ? cand : 0;
 }
 

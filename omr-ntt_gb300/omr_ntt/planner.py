@@ -198,12 +198,13 @@ def heuristic_class(p) -> int:
     """The class the planner picks without database or network (its built-in
     rule): tuned TMA kernel on the balanced split for the headline fields,
     decomposition for prefixes <= 4096, fold for strided sets, else gather."""
-    full_cls = 4 if (p["log_n"] > 12 and p["field"] in (0, 1)) else 0
+    tma_cls = {0: 8, 1: 4}  # BabyBear: two CTAs per SM; Goldilocks: double-buffered
+    full_cls = tma_cls[p["field"]] if (p["log_n"] > 12 and p["field"] in (0, 1)) else 0
     n, s = 1 << p["log_n"], point_count(p)
     if s >= n:
         return full_cls
     if p["pattern"] == "strided":
-        sub_full = 4 if (p["log_s"] > 12 and p["field"] in (0, 1)) else 0
+        sub_full = tma_cls[p["field"]] if (p["log_s"] > 12 and p["field"] in (0, 1)) else 0
         return 16 + sub_full
     if p["pattern"] == "contiguous" and s <= 4096 and n // s >= 2:
         return 12

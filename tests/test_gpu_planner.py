@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from omr_ntt import NttDomain, _lib
-from omr_ntt.fields import BabyBear, Goldilocks
+from omr_ntt.fields import BabyBear, Goldilocks, KoalaBear, TeddyBear
 from omr_ntt.inputs import gen_input_seeded, random_indices
 from gpu_util import to_dev, to_host
 
@@ -31,6 +31,11 @@ def _cands(field, log_n, pattern, count):
     (BabyBear, 18, 1, 256, 2),
     (Goldilocks, 16, 1, 4096, 1),
     (BabyBear, 16, 2, 300, 2),
+    (BabyBear, 20, 0, 50, 1),
+    (KoalaBear, 14, 0, 3, 1),
+    (TeddyBear, 15, 0, 50, 2),
+    (Goldilocks, 13, 0, 2048, 1),
+    (BabyBear, 12, 0, 1, 1),
 ], ids=str)
 def test_all_candidates_agree(oracle, field, log_n, pattern, count, batch):
     import torch
