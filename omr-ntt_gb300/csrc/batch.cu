@@ -86,10 +86,17 @@ OMR_D unsigned int ld_acquire(const unsigned int* p) {
   return v;
 }
 
+// The persistent kernel runs every line length of both fields in one body at
+// <= 128 registers: Goldilocks keeps radix-8 rounds there (radix 16 spills).
+template <class F>
+constexpr int batch_radix_log() {
+  return F::WORD == 8 ? 3 : 4;
+}
+
 template <class F, int LOGT, int C, int I>
 OMR_D void batch_col_rounds(const PassArgs<F>& a, typename F::E* s, const typename F::E* gin,
                             typename F::E* gout, int nvalid, uint32_t llo0) {
-  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  using RP = RoundPlan<LOGT, batch_radix_log<F>()>;
   if constexpr (I < RP::ROUNDS) {
     constexpr bool first = I == 0, last = I + 1 == RP::ROUNDS;
     do_round<F, LOGT, C, kBatchThreads, RP::logr(I), RP::logns(I), false,
@@ -101,7 +108,7 @@ OMR_D void batch_col_rounds(const PassArgs<F>& a, typename F::E* s, const typena
 
 template <class F, int LOGT, int C, int I>
 OMR_D void batch_row_rounds(const PassArgs<F>& a, typename F::E* s, int nvalid, uint32_t llo0) {
-  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  using RP = RoundPlan<LOGT, batch_radix_log<F>()>;
   if constexpr (I < RP::ROUNDS) {
     constexpr bool last = I + 1 == RP::ROUNDS;
     do_round<F, LOGT, C, kBatchThreads, RP::logr(I), RP::logns(I), false, SRC_SMEM,

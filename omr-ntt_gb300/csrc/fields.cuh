@@ -149,26 +149,91 @@ struct Goldilocks {
   static constexpr Tw make_tw(uint64_t w) { return Tw{w}; }
 
 #if defined(__CUDACC__)
-  OMR_D static E add(E a, E b) {
-    E s = a + b;
-    E t = s + EPS;  // s - p (mod 2^64)
-    return (s < a || s >= P) ? t : s;
-  }
+  // Canonical in, canonical out.  The carry chains are written in PTX so that
+  // a borrow or carry becomes a 0 / 0xffffffff mask that is exactly
+  // EPS = 2^64 - p in the low word (2^64 = EPS mod p).
+  OMR_D static uint64_t pack(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
+  // a - b (mod p); also valid for any a < 2^64 (result congruent, < 2^64)
   OMR_D static E sub(E a, E b) {
-    E d = a - b;
-    return a < b ? d - EPS : d;  // d + p (mod 2^64)
+    uint32_t r0, r1, m;
+    asm("sub.cc.u32 %0, %3, %5;\n\t"
+        "subc.cc.u32 %1, %4, %6;\n\t"
+        "subc.u32 %2, 0, 0;\n\t"      // borrow mask
+        "sub.cc.u32 %0, %0, %2;\n\t"  // - EPS on borrow (= + p)
+        "subc.u32 %1, %1, 0;"
+        : "=&r"(r0), "=&r"(r1), "=&r"(m)
+        : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
+    return pack(r0, r1);
   }
+  // a + b = a - (p - b): one borrow-corrected subtraction
+  OMR_D static E add(E a, E b) { return sub(a, P - b); }
   OMR_D static E neg(E a) { return a ? P - a : 0ull; }
-  OMR_D static E reduce128(uint64_t lo, uint64_t hi) {
-    uint64_t hh = hi >> 32, hl = hi & EPS;
-    uint64_t t0 = lo - hh;
-    if (lo < hh) t0 -= EPS;
-    uint64_t t1 = (hl << 32) - hl;  // hl * (2^32 - 1)
-    uint64_t t2 = t0 + t1;
-    if (t2 < t1) t2 += EPS;
-    return t2 >= P ? t2 - P : t2;
+  // a + b (2^32 - 1) - c (mod p), canonical; a, c < 2^64, b < 2^32, and
+  // a - c + 2^64 > EPS whenever a < c (true for every caller: c < 2^32, or a = 0)
+  OMR_D static E reduce3(uint64_t a, uint32_t b, uint64_t c) {
+    uint32_t r0, r1, t0, t1, m;
+    asm("sub.cc.u32 %2, %5, %8;\n\t"    // t = a - c
+        "subc.cc.u32 %3, %6, %9;\n\t"
+        "subc.u32 %4, 0, 0;\n\t"
+        "sub.cc.u32 %2, %2, %4;\n\t"    // borrow: - EPS
+        "subc.u32 %3, %3, 0;\n\t"
+        "sub.cc.u32 %0, 0, %7;\n\t"     // u = b 2^32 - b
+        "subc.u32 %1, %7, 0;\n\t"
+        "add.cc.u32 %2, %2, %0;\n\t"    // w = t + u
+        "addc.cc.u32 %3, %3, %1;\n\t"
+        "addc.u32 %4, 0, 0;\n\t"
+        "neg.s32 %4, %4;\n\t"
+        "add.cc.u32 %2, %2, %4;\n\t"    // carry: + EPS (cannot carry again)
+        "addc.u32 %3, %3, 0;\n\t"
+        "add.cc.u32 %0, %2, -1;\n\t"    // w + EPS carries  <=>  w >= p
+        "addc.cc.u32 %1, %3, 0;\n\t"
+        "addc.u32 %4, 0, 0;\n\t"
+        "{.reg .pred ge;\n\t"
+        "setp.ne.u32 ge, %4, 0;\n\t"
+        "selp.b32 %0, %0, %2, ge;\n\t"
+        "selp.b32 %1, %1, %3, ge;}"
+        : "=&r"(r0), "=&r"(r1), "=&r"(t0), "=&r"(t1), "=&r"(m)
+        : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"(b), "r"((uint32_t)c),
+          "r"((uint32_t)(c >> 32)));
+    return pack(r0, r1);
   }
-  OMR_D static E mul(E a, E b) { return reduce128(a * b, __umul64hi(a, b)); }
+  // reduce a 128-bit value hi 2^64 + lo:  2^64 = 2^32 - 1, 2^96 = -1
+  OMR_D static E reduce128(uint64_t lo, uint64_t hi) {
+    return reduce3(lo, (uint32_t)hi, hi >> 32);
+  }
+  OMR_D static E mul(E a, E b) {
+    uint32_t r0, r1, r2, r3;
+    const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b,
+                   b1 = (uint32_t)(b >> 32);
+    asm("mul.lo.u32 %0, %4, %6;\n\t"
+        "mul.hi.u32 %1, %4, %6;\n\t"
+        "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+        "madc.hi.u32 %2, %4, %7, 0;\n\t"
+        "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+        "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+        "madc.hi.u32 %3, %5, %7, 0;\n\t"
+        "mad.lo.cc.u32 %2, %5, %7, %2;\n\t"
+        "addc.u32 %3, %3, 0;"
+        : "=&r"(r0), "=&r"(r1), "=&r"(r2), "=&r"(r3)
+        : "r"(a0), "r"(a1), "r"(b0), "r"(b1));
+    return reduce3(pack(r0, r1), r2, r3);
+  }
+  // x * 2^S for a compile-time 0 <= S < 96, from shifts: x 2^S = a + b 2^64 + c 2^96
+  template <int S>
+  OMR_D static E mul_pow2(E x) {
+    static_assert(S >= 0 && S < 96, "shift out of range");
+    if constexpr (S == 0) {
+      return x;
+    } else if constexpr (S < 32) {
+      return reduce3(x << S, (uint32_t)(x >> (64 - S)), 0ull);
+    } else if constexpr (S < 64) {
+      return reduce3(x << S, (uint32_t)(x >> (64 - S)), x >> (96 - S));
+    } else if constexpr (S == 64) {
+      return reduce3(0ull, (uint32_t)x, x >> 32);
+    } else {
+      return reduce3(0ull, (uint32_t)x << (S - 64), x >> (96 - S));
+    }
+  }
   OMR_D static E mul_tw(E a, Tw t) { return mul(a, t.w); }
   OMR_D static E mont_mul(E a, E b) { return mul(a, b); }
 #endif

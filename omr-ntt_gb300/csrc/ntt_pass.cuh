@@ -92,6 +92,10 @@ struct RootConst {
   static constexpr typename F::Tw tw = F::make_tw(value);
 };
 
+// Goldilocks: 2 has order 192 (2^96 = -1), and omega_64 = 7^((p-1)/64) = 2^39,
+// so omega_R^k = 2^(39 (64/R) k mod 192) for R <= 64.
+constexpr int gl_root_exp(int logr, int k) { return (39 * (64 >> logr) * k) % 192; }
+
 // In-register R-point DFT (R = 2^LOGR), natural order in and out.
 // Radix-2 decimation in frequency: (u + v, (u - v) * omega_len^j), outputs in
 // bit-reversed register order, undone by compile-time renaming.
@@ -107,8 +111,18 @@ OMR_D void dif_stage_bf(typename F::E* v) {
     constexpr int K = J << (LOGR - LEN_LOG);
     constexpr int R = 1 << LOGR;
     constexpr int KK = INV ? ((R - K) % R) : K;
-    constexpr typename F::Tw t = RootConst<F, LOGR, KK>::tw;
-    v[BLK + J + HALF] = F::mul_tw(sub_lazy<F>(u, w), t);
+    if constexpr (F::ID == GOLDILOCKS && LOGR <= 6) {
+      // omega_R^KK = 2^E: a shift-and-fold multiply; 2^(E - 96) = -2^E swaps the difference
+      constexpr int E = gl_root_exp(LOGR, KK);
+      static_assert(hpowmod(2, E, F::p64()) == RootConst<F, LOGR, KK>::value, "root as a power of 2");
+      if constexpr (E >= 96)
+        v[BLK + J + HALF] = F::template mul_pow2<E - 96>(F::sub(w, u));
+      else
+        v[BLK + J + HALF] = F::template mul_pow2<E>(F::sub(u, w));
+    } else {
+      constexpr typename F::Tw t = RootConst<F, LOGR, KK>::tw;
+      v[BLK + J + HALF] = F::mul_tw(sub_lazy<F>(u, w), t);
+    }
   }
 }
 
@@ -172,9 +186,13 @@ struct RoundPlan {
   }
 };
 
+// Radix 16 for every field.  For Goldilocks omega_16 = -2^60, so all of a
+// round's in-register twiddles are shift-and-fold multiplies; 3 rounds of a
+// 4096-point line (instead of 4 of radix 8) drop a twiddle boundary and an
+// exchange, and 16 u64 words per thread still fit without spills.
 template <class F>
 constexpr int max_radix_log() {
-  return F::WORD == 8 ? 3 : 4;
+  return 4;
 }
 
 // Tile variants: V = 0 -> C = 32 bytes of lines (one DRAM sector per tile

@@ -1,8 +1,8 @@
 """Exact CPU emulation of the engine's pass plans (test helper).
 
 Mirrors ntt_tile_pass (omr-ntt_gb300/csrc/ntt_pass.cuh) index for index:
-tile load, the Stockham rounds of RoundPlan (radix 2^4 for 32-bit fields,
-2^3 for Goldilocks), the four-step twiddle on the store and the inverse
+tile load, the Stockham rounds of RoundPlan (radix 2^4 for every field),
+the four-step twiddle on the store and the inverse
 scale, driven by the pass records that omr_ntt_plan_passes returns.  It
 checks the host-side plan logic and the kernel's index arithmetic on the CPU.
 """
@@ -20,7 +20,7 @@ def emulate_plan(field, passes, x, log_n, inverse=False, batch=1):
     p = field.p
     N = 1 << log_n
     C = 32 // field.word_bytes
-    maxr = 3 if field.word_bytes == 8 else 4
+    maxr = 4
     wN = field.root_of_unity(log_n)
     if inverse:
         wN = pow(wN, p - 2, p)

@@ -26,6 +26,33 @@ def test_forward_all_plans_small(oracle, field):
             assert np.array_equal(back, x), (field, log_n, plan)
 
 
+def _edge_input(field, n, seed):
+    """Words at the ends of the canonical range (0, 1, p-1, p-2, (p-1)/2,
+    2^32 +- 1 for Goldilocks ...) so every carry / borrow / final-subtract
+    branch of the field arithmetic is taken."""
+    p = field.p
+    pool = [0, 1, 2, p - 1, p - 2, p - 3, (p - 1) // 2, (p + 1) // 2]
+    if p > 1 << 32:
+        pool += [(1 << 32) - 1, 1 << 32, (1 << 32) + 1, p - (1 << 32), (1 << 63), (1 << 63) - 1]
+    rng = np.random.default_rng(seed)
+    return np.array(pool, dtype=field.dtype)[rng.integers(0, len(pool), n)]
+
+
+@pytest.mark.parametrize("field", ALL, ids=lambda f: f.name)
+def test_edge_values_all_plans(oracle, field):
+    for log_n in (3, 12, 13, 16):
+        n = 1 << log_n
+        d = NttDomain(field, n)
+        x = _edge_input(field, n, log_n)
+        exp = oracle.forward(field.id, x)
+        for plan in range(omr_ntt.plan_count(field, log_n)):
+            got = omr_ntt.forward(d, x, plan=plan)
+            assert np.array_equal(got, exp), (field, log_n, plan)
+            assert np.array_equal(omr_ntt.inverse(d, got, plan=plan), x), (field, log_n, plan)
+        y = np.full(n, field.p - 1, dtype=field.dtype)  # all p - 1
+        assert np.array_equal(omr_ntt.forward(d, y), oracle.forward(field.id, y))
+
+
 @pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
 @pytest.mark.parametrize("log_n", [16, 18, 20, 22, 24])
 def test_forward_inverse_large(oracle, field, log_n):
