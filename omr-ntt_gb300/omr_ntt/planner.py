@@ -247,6 +247,17 @@ def save_model(path, mlp: Mlp, meta: dict):
     np.savez(path, params=mlp.params(), meta=json.dumps(meta))
 
 
+def save_weight_file(path, params):
+    """The network file the library loads (omr_ntt_mlp_load): "OMRM", uint32
+    n_in, n_hidden, n_out, then the float32 parameters (W1 b1 W2 b2 W3 b3)."""
+    import struct
+
+    k = (len(params) - (N_FEATURES + 1) * N_HIDDEN - (N_HIDDEN + 1) * N_HIDDEN) // (N_HIDDEN + 1)
+    with open(path, "wb") as f:
+        f.write(struct.pack("<4sIII", b"OMRM", N_FEATURES, N_HIDDEN, k))
+        f.write(np.asarray(params, dtype="<f4").tobytes())
+
+
 def load_params(path):
     z = np.load(path, allow_pickle=False)
     return z["params"], json.loads(str(z["meta"]))

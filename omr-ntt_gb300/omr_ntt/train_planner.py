@@ -3,7 +3,8 @@
     python -m omr_ntt.train_planner --points 2000 --train 1500 --out DIR
 
 Writes DIR/planner_dataset.npz (features, per-class median ms, exhaustive
-best ms, the points), DIR/planner_mlp.npz (network parameters + metadata) and
+best ms, the points), DIR/planner_mlp.npz (network parameters + metadata),
+DIR/planner_mlp.bin (the weight file the library loads) and
 prints one JSON summary: mean / median / p90 regret on the held-out points for
 the network, for the built-in heuristic, and the share of points within 5%.
 """
@@ -38,7 +39,7 @@ def main(argv=None):
         ds = {"X": z["X"], "T": z["T"], "best": z["best"]}
     else:
         ds = P.collect(pts, reps=a.reps, progress=100)
-        np.savez(os.path.join(a.out, "planner_dataset.npz"), X=ds["X"], T=ds["T"].astype(np.float32),
+        np.savez_compressed(os.path.join(a.out, "planner_dataset.npz"), X=ds["X"], T=ds["T"].astype(np.float32),
                  best=ds["best"].astype(np.float32), points=json.dumps(pts))
     t_collect = time.time() - t0
     X, T, best = ds["X"], ds["T"].astype(np.float64), ds["best"].astype(np.float64)
@@ -69,6 +70,7 @@ def main(argv=None):
     }
     P.save_model(os.path.join(a.out, "planner_mlp.npz"), mlp,
                  {"seed": a.seed, "epochs": a.epochs, "lr": a.lr, "summary": summary})
+    P.save_weight_file(os.path.join(a.out, "planner_mlp.bin"), mlp.params())
     print(json.dumps(summary), flush=True)
 
 
