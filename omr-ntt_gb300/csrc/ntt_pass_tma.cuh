@@ -409,18 +409,20 @@ __global__ void __launch_bounds__(NT, 3 - NBUF)
   }
 }
 
-// Thread count of the TMA pass: EPT elements per thread.  16 keeps a
-// 32-bit-field thread at <= 64 registers, so a 4096-point tile runs as two
-// 512-thread CTAs per SM (NBUF = 1) whose barriers interleave; measured on
-// GB300 that beats 32 elements per thread (16 warps per SM) by ~11%.
-template <class F>
+// Thread count of the TMA pass: EPT elements per thread.  For 32-bit fields
+// at 2048- and 4096-point lines, 16 keeps a thread at <= 64 registers, so a
+// tile runs as two 512-thread CTAs per SM (NBUF = 1) whose barriers
+// interleave; measured on GB300 that beats 32 elements per thread (16 warps
+// per SM) by ~11% at n = 2^24.  Shorter lines keep 32 (their CTAs are small
+// already; 16 was ~20% slower on the 1024-point column pass).
+template <class F, int LOGT>
 constexpr int tma_ept() {
-  return 16;
+  return F::WORD == 8 ? 16 : (LOGT >= 11 ? 16 : 32);
 }
 template <class F, int LOGT, int NBUF>
 constexpr int tma_threads() {
   constexpr int TC = (1 << LOGT) * tma_cols<F>();
-  constexpr int nt = TC / (tma_ept<F>() * (3 - NBUF));
+  constexpr int nt = TC / (tma_ept<F, LOGT>() * (3 - NBUF));
   return nt < 128 ? 128 : (nt > 1024 ? 1024 : nt);
 }
 
