@@ -133,6 +133,47 @@ def cpu_baseline(field, log_n, seconds, steps=None):
     return n * len(times) / sum(times) / 1e9, cores, len(times), times
 
 
+def cpu_config_samples(extras, partial, headline_ms, field, log_n):
+    """Each BASELINE shape timed on the host cores with the oracle's C
+    restatement of the reference encoder the crate's benches use for it
+    (ArkRadix2 at 2^16, TfheStockhamRadix8 and WinterfellFourStep at 2^24,
+    WinterfellFourStep on the 64 x 2^20 batch, TransformDecomposition for
+    prefixes at 2^22), beside the GPU milliseconds of the same shape."""
+    from omr_ntt.fields import BabyBear, Goldilocks
+    from oracle import oracle
+
+    oracle.set_threads(0)
+    cores = oracle.get_threads()
+    out = {"cores": cores, "kind": "port", "rows": {}}
+
+    def best_ms(fn, reps=2):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return 1000 * min(ts)
+
+    gpu = {f"{field.name} fwd 2^{log_n}x1": headline_ms}
+    gpu.update({k: v["ms"] for k, v in extras.items()})
+    rows = [("BabyBear fwd 2^16x1", BabyBear, 16, 1, "ArkRadix2", 0),
+            ("BabyBear fwd 2^24x1", BabyBear, 24, 1, "TfheStockhamRadix8", 0),
+            ("BabyBear fwd 2^24x1 (four-step)", BabyBear, 24, 1, "WinterfellFourStep", 0),
+            ("Goldilocks fwd 2^24x1", Goldilocks, 24, 1, "WinterfellFourStep", 0),
+            ("BabyBear fwd 2^20x64", BabyBear, 20, 64, "WinterfellFourStep", 0)]
+    for k in (4, 8, 12, 16):
+        rows.append((f"BabyBear s=2^{k} prefix", BabyBear, 22, 1, "TransformDecomposition", 1 << (k - 1)))
+    for label, fld, lg, bt, enc, s in rows:
+        x = __import__("omr_ntt").gen_input_seeded(fld, (1 << lg) * bt, 7)
+        ms = best_ms(lambda: oracle.ntt(fld.id, x, enc, s=s, batch=bt), reps=1 if lg + (bt > 1) * 6 >= 24 else 3)
+        key = label.replace(" (four-step)", "")
+        g = partial.get(fld.name, {}).get(label.split(" ", 1)[1]) if "prefix" in label else gpu.get(key)
+        out["rows"][label] = {"encoder": enc, "cpu_ms": round(ms, 3), "gpu_ms": g,
+                              "gpu_speedup": round(ms / g, 1) if g else None}
+    return out
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
@@ -292,7 +333,7 @@ def main():
                 ts.append(e0.elapsed_time(e1))
             return sum(ts) / len(ts)
 
-        for fld, lg, bt, inv in ((BabyBear, 24, 1, True), (Goldilocks, 24, 1, False),
+        for fld, lg, bt, inv in ((BabyBear, 16, 1, False), (BabyBear, 24, 1, True), (Goldilocks, 24, 1, False),
                                  (Goldilocks, 24, 1, True), (BabyBear, 20, 64, False),
                                  (Goldilocks, 20, 64, False), (BabyBear, 22, 1, False),
                                  (BabyBear, 20, 1, False), (BabyBear, 27, 1, False)):
@@ -402,6 +443,12 @@ def main():
                "sample": f"{cnt} x WinterfellFourStep {field.name} n=2^{log_n} forward, C restatement "
                          f"of src/encoders/winterfell_four_step.rs, OpenMP {cores} threads"}
 
+    # ---- CPU restatements of the reference's own encoders on the other configs
+    # (rank 0, N=1): one bounded sample each, beside the GPU time of the same shape
+    cpu_configs = None
+    if not args.no_extras and rank == 0 and world == 1:
+        cpu_configs = cpu_config_samples(extras, partial, ms_per_step, field, log_n)
+
     if rank == 0:
         clocks = clk.summary()
         line = {
@@ -428,6 +475,7 @@ def main():
             "clocks": clocks,
             "extras": extras,
             "partial_ms": partial,
+            "cpu_configs": cpu_configs,
             "mixed_batch": mixed,
             "learned_planner": learned,
         }
