@@ -149,6 +149,18 @@ std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
     splits.push_back(s);
     std::vector<int> r(s.rbegin(), s.rend());
     if (r != s) splits.push_back(r);
+    if (P == pmin && P >= 2) {
+      // uneven splits (remainder, 4096, ..., 4096) and (4096, ..., 4096,
+      // remainder): most of the work runs in the 4096-point TMA pass (e.g.
+      // 4096 x 1024 at 2^22, the fastest BabyBear plan there)
+      std::vector<int> g(P, kMaxLogT);
+      g[0] = (int)log_n - kMaxLogT * (P - 1);
+      if (g[0] >= 1 && g != s && g != r) {
+        splits.push_back(g);
+        std::vector<int> gr(g.rbegin(), g.rend());
+        if (gr != g) splits.push_back(gr);
+      }
+    }
   }
   for (int v = 0; v < 3; v++)
     for (auto& s : splits) {

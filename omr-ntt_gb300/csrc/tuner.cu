@@ -63,7 +63,9 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
 
 // ------------------------------------------------------------------ plan classes
 // A fixed, size-independent plan vocabulary for the learned planner:
-//   0..11   full transform: (pass-count offset 0/1, balanced/reversed split) x kernel variant 0..2
+//   0..11   full transform: split kind x kernel variant 0..2 (class = 4 variant + kind);
+//           kind 0: balanced split with the fewest passes, 1: its reverse,
+//           2: balanced with one more pass, 3: large-first (4096, ..., 4096, remainder)
 //   12..15  prefix decomposition with line length next_pow2(count) << j, j = 0..3
 //   16..27  strided fold, then the count-point transform with full class (c - 16)
 //   28..39  full transform with full class (c - 28), then gather
@@ -73,17 +75,23 @@ constexpr int kNumClasses = 40;
 static int full_class_plan(uint32_t log_n, int fc) {
   const auto plans = enumerate_plans(log_n);
   if (log_n == 0) return fc == 0 ? 0 : -1;
-  const int variant = fc / 4, po = (fc % 4) / 2, rev = fc % 2;
+  const int variant = fc / 4, kind = fc % 4;
   const int pmin = std::max<int>(1, (int)((log_n + kMaxLogT - 1) / kMaxLogT));
-  const int P = pmin + po;
+  const int P = pmin + (kind == 2 ? 1 : 0);
   if ((uint32_t)P > log_n || P > 3) return -1;
   std::vector<int> bal(P);
   for (int i = 0; i < P; i++) bal[i] = (int)(log_n / P) + (i < (int)(log_n % P) ? 1 : 0);
   if (bal[0] > kMaxLogT) return -1;
   std::vector<int> want = bal;
-  if (rev) {
+  if (kind == 1) {
     std::reverse(want.begin(), want.end());
     if (want == bal) return -1;  // same as the balanced class
+  } else if (kind == 3) {
+    if (P < 2) return -1;
+    std::fill(want.begin(), want.end(), kMaxLogT);
+    want[P - 1] = (int)log_n - kMaxLogT * (P - 1);
+    std::vector<int> rev(bal.rbegin(), bal.rend());
+    if (want[P - 1] < 1 || want == bal || want == rev) return -1;  // same as another class
   }
   if (P == 1 && variant > 0) return -1;  // single-pass plans have one kernel
   for (int i = 0; i < (int)plans.size(); i++)

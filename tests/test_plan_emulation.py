@@ -78,8 +78,9 @@ def test_tma_pass_preconditions():
                         if p["logT"] < 8 or p["twiddle"] == 0 and p["es_in"] != 1:
                             continue
                         if p["is_lo"] == 1:  # column pass
+                            if (p["L_lo"] * w) % 16:
+                                continue  # fewer than 16 bytes of columns: the plain tile pass runs it
                             assert p["es_in"] == p["L_lo"]
-                            assert (p["L_lo"] * w) % 16 == 0
                             assert T * p["L_m"] * p["L_b"] < 2 ** 32
                         else:  # row pass
                             for stride in (p["is_lo"], p["is_m"], p["is_b"]):
