@@ -145,9 +145,18 @@ int mlp_select_class(int field, uint32_t log_n, uint64_t batch, int pattern, uin
 
 static bool g_use_mlp = false;
 
+// The network is trusted only inside the domain it was trained on: log2 n in
+// [10, 24], batch <= 512, batch * n <= 2^26 words.  Outside it the planner
+// falls back to the built-in rule (a 2^27 transform is not extrapolated).
+constexpr uint32_t kMlpMinLogN = 10, kMlpMaxLogN = 24;
+constexpr uint64_t kMlpMaxBatch = 512, kMlpMaxWords = 1ull << 26;
+
 static bool mlp_choice(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
                        Cand* out) {
   if (!g_use_mlp) return false;
+  if (log_n < kMlpMinLogN || log_n > kMlpMaxLogN || batch > kMlpMaxBatch ||
+      (batch << log_n) > kMlpMaxWords)
+    return false;
   bool app[kNumClasses];
   Cand cands[kNumClasses];
   bool any = false;
