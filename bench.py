@@ -49,6 +49,27 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
+def job_throughput(local_ms, elems_per_step, steps, world, device=None):
+    """Whole-job throughput of replicas (weak scaling): every rank transforms
+    its own `steps` x `elems_per_step` words with no data exchange, the job
+    time is the slowest rank's, so value = all ranks' elements / max time
+    (Gelem/s).  Returns (value, max_ms); the only collective is the MAX."""
+    total_ms = float(local_ms)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return elems_per_step * world * steps / (total_ms / 1e3) / 1e9, total_ms
+
+
+def replica_seed(rank):
+    """Each replica transforms its own seeded input."""
+    return 42 + rank
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -235,7 +256,7 @@ def main():
     w = field.word_bytes
     sdt = torch.int32 if w == 4 else torch.int64
     domain = NttDomain(field, n)
-    x = omr_ntt.gen_input_seeded(field, n, 42 + rank)
+    x = omr_ntt.gen_input_seeded(field, n, replica_seed(rank))
     xd = torch.from_numpy(x.view(np.int32 if w == 4 else np.int64).copy()).cuda()
     buf = xd.clone()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -268,12 +289,7 @@ def main():
         torch.cuda.synchronize()
     barrier()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = n * world * args.steps / (total_ms / 1e3) / 1e9
+    value, total_ms = job_throughput(sum(step_ms), n, args.steps, world, device="cuda")
     ms_per_step = total_ms / args.steps
 
     # ---- per-pass timing (the dominant kernel's roofline), same stream, CUDA events
