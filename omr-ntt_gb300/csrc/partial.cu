@@ -31,7 +31,8 @@ constexpr int prefix_cols() {  // ~64 KiB tile, rows of >= 16 bytes, <= 256 colu
 template <class F, int LOGT>
 constexpr int prefix_threads() {  // <= 256 threads at <= 128 registers: two CTAs per SM
   constexpr int tc = (1 << LOGT) * prefix_cols<F, LOGT>();
-  constexpr int nt = tc / tile_ept<F>();
+  // short lines (one round) take 16 words a thread: more warps for the loads
+  constexpr int nt = tc / (LOGT <= 4 ? 16 : tile_ept<F>());
   return nt < 64 ? 64 : (nt > 256 ? 256 : nt);
 }
 
@@ -161,8 +162,17 @@ __global__ void __launch_bounds__(kReduceThreads)
   const uint32_t c = blockIdx.x * cw + threadIdx.x % cw;
   E acc = 0;
   if (c < cols) {
-#pragma unroll 4
-    for (uint32_t r = slice; r < rows; r += slices) acc = F::add(acc, partial[(uint64_t)r * cols + c]);
+    // eight predicated loads in flight per step
+    for (uint32_t r = slice; r < rows; r += 8 * slices) {
+      E v[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const uint32_t rr = r + k * slices;
+        v[k] = rr < rows ? partial[(uint64_t)rr * cols + c] : (E)0;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) acc = F::add(acc, v[k]);
+    }
   }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -340,6 +350,64 @@ __global__ void __launch_bounds__(256) fold_flat_kernel(const typename F::E* __r
   }
 }
 
+// Strided fold with 16-byte loads.  Every thread reads VW = 16 / w adjacent
+// words per load, eight loads in flight.  The grid stride is a multiple of
+// count (count a power of two <= 4096; gridDim a multiple of 4 and of
+// count / CH), so each of a thread's VW lanes stays in one column.  The CTA
+// then sums the CH = 256 VW positions of its chunk down to columns in shared
+// memory:
+//   count <= CH: one row of count column sums per CTA;
+//   count >  CH: the CTA's chunk is CH consecutive columns of one row
+//               (row = blockIdx / (count / CH)).
+constexpr int kFoldThreads = 256;
+template <class F>
+__global__ void __launch_bounds__(kFoldThreads) fold_vec_kernel(const typename F::E* __restrict__ x,
+                                                                uint64_t n, uint32_t count,
+                                                                typename F::E* __restrict__ partial) {
+  using E = typename F::E;
+  constexpr int VW = 16 / F::WORD;
+  constexpr int CH = kFoldThreads * VW;  // words per CTA per sweep step
+  __shared__ E red[CH];
+  const uint64_t stride = (uint64_t)gridDim.x * CH;
+  E acc[VW];
+#pragma unroll
+  for (int u = 0; u < VW; u++) acc[u] = 0;
+  const uint4* __restrict__ xv = reinterpret_cast<const uint4*>(x);
+  uint64_t i = (uint64_t)blockIdx.x * CH + (uint64_t)threadIdx.x * VW;
+  // eight predicated loads per step, all issued before the adds (a zero
+  // vector past the end adds nothing)
+  for (; i < n; i += 8 * stride) {
+    uint4 q[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const uint64_t j = i + k * stride;
+      q[k] = j < n ? xv[j / VW] : make_uint4(0u, 0u, 0u, 0u);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const E* w = reinterpret_cast<const E*>(&q[k]);
+#pragma unroll
+      for (int u = 0; u < VW; u++) acc[u] = F::add(acc[u], w[u]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < VW; u++) red[threadIdx.x * VW + u] = acc[u];
+  __syncthreads();
+  // position p of the chunk holds column (blockIdx * CH + p) mod count
+  for (uint32_t h = CH / 2; h >= count && h >= 1; h >>= 1) {
+    for (uint32_t p = threadIdx.x; p < h; p += kFoldThreads) red[p] = F::add(red[p], red[p + h]);
+    __syncthreads();
+  }
+  if (count <= (uint32_t)CH) {
+    for (uint32_t c = threadIdx.x; c < count; c += kFoldThreads)
+      partial[(uint64_t)blockIdx.x * count + c] = red[c];
+  } else {
+    const uint32_t per = count / CH;
+    E* row = partial + (uint64_t)(blockIdx.x / per) * count + (uint64_t)(blockIdx.x % per) * CH;
+    for (uint32_t p = threadIdx.x; p < (uint32_t)CH; p += kFoldThreads) row[p] = red[p];
+  }
+}
+
 template <class F>
 static int run_fold(omr_ntt_domain_s* d, int sub_plan, uint64_t count, const void* in, void* out,
                     cudaStream_t stream) {
@@ -358,7 +426,21 @@ static int run_fold(omr_ntt_domain_s* d, int sub_plan, uint64_t count, const voi
   if (rc) return rc;
   E* part = static_cast<E*>(buf);
   uint64_t nch = 0;
-  if (count <= 4096 && d->n >= 256ull * 1216) {
+  const int vw = 16 / (int)w;
+  const uint64_t ch = (uint64_t)kFoldThreads * vw;
+  if (count <= 4096 && d->n >= ch * 4 && !(reinterpret_cast<uintptr_t>(in) & 15)) {
+    // 16-byte loads: four CTAs per SM, a multiple of 4 (and of
+    // count / CH), never more than the sweep needs
+    uint64_t g = (uint64_t)device_sm_count(d->device) * 4;
+    const uint64_t need = d->n / ch;
+    if (g > need) g = need;
+    const uint64_t m = count / ch > 4 ? count / ch : 4;  // grid stride a multiple of count
+    g = g < m ? m : g & ~(m - 1);
+    const uint32_t grid = (uint32_t)g;
+    fold_vec_kernel<F><<<grid, kFoldThreads, 0, stream>>>(static_cast<const E*>(in), d->n, (uint32_t)count, part);
+    OMR_CUDA_TRY(cudaGetLastError());
+    nch = count > ch ? grid / (count / ch) : grid;
+  } else if (count <= 4096 && d->n >= 256ull * 1216) {
     const uint32_t grid = 1216;  // 8 CTAs per SM; a multiple of count / 256 for count <= 4096
     fold_flat_kernel<F><<<grid, 256, 0, stream>>>(static_cast<const E*>(in), d->n, (uint32_t)count, part);
     OMR_CUDA_TRY(cudaGetLastError());

@@ -4,6 +4,8 @@ log N = 27: two warm-up calls, then timed calls on seed 42).
 
     python -m omr_ntt.profile_ntt                              # the reference's case
     python -m omr_ntt.profile_ntt --mode forward --field BabyBear --log-n 24 --plan -1 --iters 2
+    python -m omr_ntt.profile_ntt --mode partial --log-n 22 --pattern 1 --s 16
+    python -m omr_ntt.profile_ntt --mode batch --requests 512   # mixed batch, graph launch
 
 Runs on device buffers through the C ABI with no host copies in the loop, so
 that a profiler sees only the engine's kernels (plus one buffer fill).
@@ -19,7 +21,7 @@ from .fields import field_by_name
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--mode", default="encode", choices=["encode", "forward", "inverse", "partial"])
+    ap.add_argument("--mode", default="encode", choices=["encode", "forward", "inverse", "partial", "batch"])
     ap.add_argument("--field", default="BabyBear")
     ap.add_argument("--log-n", type=int, default=27)
     ap.add_argument("--encoder", default="TransformDecomposition")
@@ -28,9 +30,13 @@ def main(argv=None):
     ap.add_argument("--plan", type=int, default=-1)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--iters", type=int, default=5)
+    ap.add_argument("--requests", type=int, default=512)
     a = ap.parse_args(argv)
 
     import torch
+
+    if a.mode == "batch":
+        return run_batch(a)
 
     from . import NttDomain, encoders
 
@@ -48,6 +54,12 @@ def main(argv=None):
                                     encoders.TfheStockhamRadix8, encoders.TransformDecomposition,
                                     encoders.TransformDecompositionV2, encoders.WinterfellFourStep)}
 
+    idx = None
+    if a.mode == "partial" and a.pattern == 2:
+        from .inputs import random_indices
+
+        idx = torch.from_numpy(random_indices(n, a.s, 3).view("int32")).cuda()
+
     def once():
         p = ctypes.c_void_p(x.data_ptr())
         if a.mode == "encode":
@@ -59,7 +71,8 @@ def main(argv=None):
         elif a.mode == "inverse":
             _lib.check(L.omr_ntt_inverse(d.handle, a.plan, p, p, 1, st))
         else:
-            _lib.check(L.omr_ntt_partial(d.handle, a.pattern, a.s, None, p, ctypes.c_void_p(out.data_ptr()), st))
+            ip = ctypes.c_void_p(idx.data_ptr()) if idx is not None else None
+            _lib.check(L.omr_ntt_partial(d.handle, a.pattern, a.s, ip, p, ctypes.c_void_p(out.data_ptr()), st))
 
     for _ in range(a.warmup):
         once()
@@ -67,6 +80,29 @@ def main(argv=None):
     for _ in range(a.iters):
         once()
     torch.cuda.synchronize()
+    print("ok")
+
+
+def run_batch(a):
+    """The mixed batch of the bench (log n in [10, 20], both fields, 25%
+    partial, fwd/inv) with `--requests` requests: one graph-launched
+    persistent kernel per run."""
+    import torch
+
+    from .batch import Batch, layout, mixed_requests
+
+    reqs = mixed_requests(2024, count=a.requests)
+    ib, ob = layout(reqs)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    d_in = torch.randint(0, 1 << 30, ((ib + 3) // 4,), dtype=torch.int32, device="cuda", generator=g)
+    d_out = torch.empty(ob, dtype=torch.uint8, device="cuda")
+    bt = Batch(reqs)
+    st = torch.cuda.current_stream().cuda_stream
+    for _ in range(a.warmup + a.iters):
+        bt.run(d_in.data_ptr(), d_out.data_ptr(), st)
+    torch.cuda.synchronize()
+    bt.check(st)
+    bt.close()
     print("ok")
 
 

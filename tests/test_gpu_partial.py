@@ -68,3 +68,25 @@ def test_host_api_and_edges(case):
         omr_ntt.partial(d, x, STRIDED, 3)
     with pytest.raises(OmrNttError):
         omr_ntt.partial(d, x, PREFIX, d.N + 1)
+
+
+def test_strided_from_an_unaligned_pointer(oracle):
+    """A device input that starts 4 bytes into an allocation (not 16-byte
+    aligned) takes the scalar fold path and gives the same words."""
+    import ctypes
+
+    import torch
+    from omr_ntt import _lib
+
+    f, n = BabyBear, 1 << 16
+    x = gen_input_seeded(f, n, 77)
+    full = oracle.forward(f.id, x)
+    d = NttDomain(f, n)
+    big = torch.zeros(n + 4, dtype=torch.int32, device="cuda")
+    big[1:n + 1] = torch.from_numpy(x.view(np.int32)).cuda()
+    for s in (16, 256, 4096):
+        out = torch.zeros(s, dtype=torch.int32, device="cuda")
+        _lib.check(_lib.lib().omr_ntt_partial(d.handle, STRIDED, s, None, ctypes.c_void_p(big.data_ptr() + 4),
+                                              ctypes.c_void_p(out.data_ptr()), None))
+        torch.cuda.synchronize()
+        assert np.array_equal(to_host(out, f.dtype), full[::n // s]), s

@@ -36,6 +36,10 @@ def _cands(field, log_n, pattern, count):
     (TeddyBear, 15, 0, 50, 2),
     (Goldilocks, 13, 0, 2048, 1),
     (BabyBear, 12, 0, 1, 1),
+    (BabyBear, 13, 1, 4096, 1),
+    (Goldilocks, 14, 1, 2, 1),
+    (KoalaBear, 12, 1, 1, 2),
+    (Goldilocks, 20, 1, 16, 1),
 ], ids=str)
 def test_all_candidates_agree(oracle, field, log_n, pattern, count, batch):
     import torch
