@@ -155,13 +155,14 @@ struct Goldilocks {
   OMR_D static uint64_t pack(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
   // a - b (mod p); also valid for any a < 2^64 (result congruent, < 2^64)
   OMR_D static E sub(E a, E b) {
-    uint32_t r0, r1, m;
-    asm("sub.cc.u32 %0, %3, %5;\n\t"
-        "subc.cc.u32 %1, %4, %6;\n\t"
-        "subc.u32 %2, 0, 0;\n\t"      // borrow mask
-        "sub.cc.u32 %0, %0, %2;\n\t"  // - EPS on borrow (= + p)
-        "subc.u32 %1, %1, 0;"
-        : "=&r"(r0), "=&r"(r1), "=&r"(m)
+    uint32_t r0, r1;
+    asm("{.reg .u32 m;\n\t"
+        "sub.cc.u32 %0, %2, %4;\n\t"
+        "subc.cc.u32 %1, %3, %5;\n\t"
+        "subc.u32 m, 0, 0;\n\t"       // borrow mask
+        "sub.cc.u32 %0, %0, m;\n\t"   // - EPS on borrow (= + p)
+        "subc.u32 %1, %1, 0;}"
+        : "=&r"(r0), "=&r"(r1)
         : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
     return pack(r0, r1);
   }
@@ -171,28 +172,29 @@ struct Goldilocks {
   // a + b (2^32 - 1) - c (mod p), canonical; a, c < 2^64, b < 2^32, and
   // a - c + 2^64 > EPS whenever a < c (true for every caller: c < 2^32, or a = 0)
   OMR_D static E reduce3(uint64_t a, uint32_t b, uint64_t c) {
-    uint32_t r0, r1, t0, t1, m;
-    asm("sub.cc.u32 %2, %5, %8;\n\t"    // t = a - c
-        "subc.cc.u32 %3, %6, %9;\n\t"
-        "subc.u32 %4, 0, 0;\n\t"
-        "sub.cc.u32 %2, %2, %4;\n\t"    // borrow: - EPS
-        "subc.u32 %3, %3, 0;\n\t"
-        "sub.cc.u32 %0, 0, %7;\n\t"     // u = b 2^32 - b
-        "subc.u32 %1, %7, 0;\n\t"
-        "add.cc.u32 %2, %2, %0;\n\t"    // w = t + u
-        "addc.cc.u32 %3, %3, %1;\n\t"
-        "addc.u32 %4, 0, 0;\n\t"
-        "neg.s32 %4, %4;\n\t"
-        "add.cc.u32 %2, %2, %4;\n\t"    // carry: + EPS (cannot carry again)
-        "addc.u32 %3, %3, 0;\n\t"
-        "add.cc.u32 %0, %2, -1;\n\t"    // w + EPS carries  <=>  w >= p
-        "addc.cc.u32 %1, %3, 0;\n\t"
-        "addc.u32 %4, 0, 0;\n\t"
-        "{.reg .pred ge;\n\t"
-        "setp.ne.u32 ge, %4, 0;\n\t"
-        "selp.b32 %0, %0, %2, ge;\n\t"
-        "selp.b32 %1, %1, %3, ge;}"
-        : "=&r"(r0), "=&r"(r1), "=&r"(t0), "=&r"(t1), "=&r"(m)
+    uint32_t r0, r1;
+    asm("{.reg .u32 t0, t1, m;\n\t"
+        ".reg .pred ge;\n\t"
+        "sub.cc.u32 t0, %2, %5;\n\t"    // t = a - c
+        "subc.cc.u32 t1, %3, %6;\n\t"
+        "subc.u32 m, 0, 0;\n\t"
+        "sub.cc.u32 t0, t0, m;\n\t"     // borrow: - EPS
+        "subc.u32 t1, t1, 0;\n\t"
+        "sub.cc.u32 %0, 0, %4;\n\t"     // u = b 2^32 - b
+        "subc.u32 %1, %4, 0;\n\t"
+        "add.cc.u32 t0, t0, %0;\n\t"    // w = t + u
+        "addc.cc.u32 t1, t1, %1;\n\t"
+        "addc.u32 m, 0, 0;\n\t"
+        "neg.s32 m, m;\n\t"
+        "add.cc.u32 t0, t0, m;\n\t"     // carry: + EPS (cannot carry again)
+        "addc.u32 t1, t1, 0;\n\t"
+        "add.cc.u32 %0, t0, -1;\n\t"    // w + EPS carries  <=>  w >= p
+        "addc.cc.u32 %1, t1, 0;\n\t"
+        "addc.u32 m, 0, 0;\n\t"
+        "setp.ne.u32 ge, m, 0;\n\t"
+        "selp.b32 %0, %0, t0, ge;\n\t"
+        "selp.b32 %1, %1, t1, ge;}"
+        : "=&r"(r0), "=&r"(r1)
         : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"(b), "r"((uint32_t)c),
           "r"((uint32_t)(c >> 32)));
     return pack(r0, r1);

@@ -323,9 +323,10 @@ __global__ void __launch_bounds__(NT, 3 - NBUF)
                       const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
   using E = typename F::E;
   using Tw = typename F::Tw;
-  constexpr int T = 1 << LOGT;
   constexpr size_t BW = tma_buf_words<F, LOGT, C>();
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // declared with the same alignment as the other kernels' dynamic shared
+  // memory; the buffers are aligned to 128 bytes below
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ int abort_flag;
   // align by pointer arithmetic on the shared array (keeps the state space)

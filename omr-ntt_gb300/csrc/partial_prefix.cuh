@@ -1,0 +1,282 @@
+// partial_prefix.cuh -- the pruned prefix transform and the row reduction
+// shared by the partial-output paths.  launch_prefix<F> is instantiated once
+// per field in partial_prefix_<field>.cu (parallel compiles); every other
+// translation unit sees the extern declarations below.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "partial.cuh"
+
+namespace omr {
+
+// ---------------------------------------------------------------- prefix
+// Pruned prefix transform (the reference's TransformDecomposition,
+// src/encoders/transform_decomposition.rs:25-97, with n1 = T >= m):
+//   X[k] = sum_{r < N/T} omega_N^(r k) * Y_r[k],  Y_r = DFT_T(x[r + (N/T) c] over c),  k < m.
+// Each CTA owns a contiguous run of groups of C adjacent columns r.  Per group
+// it runs the T-point Stockham rounds of the tile pass (the first round reads
+// global memory straight into registers) into a shared-memory tile, then
+// folds the group into per-thread accumulators by Horner's rule over the
+// columns: thread (k, slice) visits columns r_i = r_first + slice + TPK i
+// (TPK column slices), acc = acc * omega_N^(-TPK k) + Y_{r_i}[k], and at the
+// end multiplies by omega_N^(k r_last); so sum_i omega_N^(k r_i) Y_{r_i}[k]
+// costs one constant multiply and one add per needed output and column,
+// with no per-element twiddle lookups.  The slices are combined in shared
+// memory, one row of m words per CTA, and a row-reduction kernel sums the
+// rows.  The input is read once.
+template <class F, int LOGT>
+constexpr int prefix_cols() {  // ~64 KiB tile, rows of >= 16 bytes, <= 256 columns
+  constexpr int lo = 16 / F::WORD;
+  constexpr int c = (65536 / F::WORD) >> LOGT;
+  return c < lo ? lo : (c > 256 ? 256 : c);
+}
+template <class F, int LOGT>
+constexpr int prefix_threads() {  // <= 256 threads at <= 128 registers: two CTAs per SM
+  constexpr int tc = (1 << LOGT) * prefix_cols<F, LOGT>();
+  // short lines (one round) take 16 words a thread: more warps for the loads
+  constexpr int nt = tc / (LOGT <= 4 ? 16 : tile_ept<F>());
+  return nt < 64 ? 64 : (nt > 256 ? 256 : nt);
+}
+
+template <class F, int LOGT, int C, int NT, int I>
+OMR_D void prefix_rounds(const PassArgs<F>& a, typename F::E* s, const typename F::E* gin,
+                         int nvalid) {
+  using RP = RoundPlan<LOGT, max_radix_log<F>()>;
+  if constexpr (I < RP::ROUNDS) {
+    constexpr int SRC = I == 0 ? SRC_GLOBAL : SRC_SMEM;
+    do_round<F, LOGT, C, NT, RP::logr(I), RP::logns(I), false, SRC, DST_SMEM, false, false>(
+        a, s, gin, nullptr, nvalid, 0, 0);
+    prefix_rounds<F, LOGT, C, NT, I + 1>(a, s, gin, nvalid);
+  }
+}
+
+// omega_N^e in "twiddle-Montgomery" form (what mul_m takes) from the
+// two-level four-step tables.
+template <class F>
+OMR_D typename F::E omega_m(const PassArgs<F>& a, uint64_t e) {
+  const uint32_t ee = (uint32_t)e & a.tw_mask;
+  return F::mul_tw(a.tw_lo[ee & ((1u << kTwLoBits) - 1)], a.tw_hi[ee >> kTwLoBits]);
+}
+// omega_N^e as a twiddle operand for mul_tw.
+template <class F>
+OMR_D typename F::Tw omega_tw(const PassArgs<F>& a, uint64_t e) {
+  const typename F::E wm = omega_m<F>(a, e);
+  if constexpr (F::ID == GOLDILOCKS) {
+    return F::make_tw(wm);
+  } else {
+    return F::make_tw(F::mont(wm, 1u));  // canonical omega^e
+  }
+}
+
+template <class F, int LOGT>
+__global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
+    prefix_decomp_kernel(const PassArgs<F> a, uint32_t m, typename F::E* __restrict__ partial) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int T = 1 << LOGT;
+  constexpr int C = prefix_cols<F, LOGT>();
+  constexpr int NT = prefix_threads<F, LOGT>();
+  constexpr int KMAX = T > NT ? T / NT : 1;  // outputs per thread when m > NT
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  E* s = reinterpret_cast<E*>(smem_raw);
+
+  // thread -> KACT adjacent outputs x TPK column slices (m <= NT), or
+  // outputs k = t + j NT (m > NT, one slice)
+  uint32_t kact = 1;
+  while (kact < m && kact < (uint32_t)NT) kact <<= 1;
+  const uint32_t tpk = min((uint32_t)NT / kact, (uint32_t)C);
+  const uint32_t kper = (m + NT - 1) / NT;
+  const uint32_t kbase = threadIdx.x % kact;
+  const uint32_t slice = threadIdx.x / kact;
+  const bool active = slice < tpk;
+
+  E acc[KMAX];
+  Tw zi[KMAX];
+#pragma unroll
+  for (int j = 0; j < KMAX; j++) {
+    acc[j] = 0;
+    const uint32_t k = kbase + j * NT;
+    zi[j] = omega_tw<F>(a, (uint64_t)0 - (uint64_t)tpk * k);  // omega_N^(-TPK k)
+  }
+
+  const uint32_t groups = (a.L_lo + C - 1) / C;
+  const uint32_t g0 = (uint32_t)((uint64_t)blockIdx.x * groups / gridDim.x);
+  const uint32_t g1 = (uint32_t)((uint64_t)(blockIdx.x + 1) * groups / gridDim.x);
+  for (uint32_t g = g0; g < g1; g++) {
+    const uint32_t llo0 = g * C;
+    const int nvalid = (int)min((uint32_t)C, a.L_lo - llo0);
+    prefix_rounds<F, LOGT, C, NT, 0>(a, s, a.in + llo0, nvalid);
+    if (active) {
+#pragma unroll
+      for (int j = 0; j < KMAX; j++) {
+        const uint32_t k = kbase + j * NT;
+        if (j < (int)kper && k < m) {
+          E h = acc[j];
+#pragma unroll 4
+          for (uint32_t c = slice; c < (uint32_t)C; c += tpk)
+            h = F::add(F::mul_tw(h, zi[j]), s[tile_idx<F, C>((int)k, (int)c)]);
+          acc[j] = h;
+        }
+      }
+    }
+    __syncthreads();  // the next group's first round overwrites the tile
+  }
+  if (g1 > g0) {
+    const uint64_t r_last = (uint64_t)(g1 - 1) * C + (C - tpk) + slice;
+#pragma unroll
+    for (int j = 0; j < KMAX; j++) {
+      const uint32_t k = kbase + j * NT;
+      if (active && j < (int)kper && k < m) acc[j] = mul_m<F>(acc[j], omega_m<F>(a, r_last * k));
+    }
+  }
+  if (tpk > 1) {
+    // combine the slices of every output: s[slice * kact + k]
+    if (active) s[slice * kact + kbase] = acc[0];
+    __syncthreads();
+    if (threadIdx.x < m) {
+      E sum = 0;
+      for (uint32_t sl = 0; sl < tpk; sl++) sum = F::add(sum, s[sl * kact + threadIdx.x]);
+      partial[(uint64_t)blockIdx.x * m + threadIdx.x] = sum;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < KMAX; j++) {
+      const uint32_t k = threadIdx.x + j * NT;
+      if (j < (int)kper && k < m) partial[(uint64_t)blockIdx.x * m + k] = acc[j];
+    }
+  }
+}
+
+// out[k] = sum over rows of partial[row * cols + k].  A CTA of kReduceThreads
+// covers cw adjacent columns (cw a power of two <= 32) with kReduceThreads / cw
+// row slices, so each thread sums only rows / slices values (independent
+// loads, no long serial chain) before a shared-memory tree over the slices.
+constexpr int kReduceThreads = 1024;
+
+template <class F>
+__global__ void __launch_bounds__(kReduceThreads)
+    reduce_rows_kernel(const typename F::E* __restrict__ partial, uint32_t rows, uint32_t cols,
+                       uint32_t cw, typename F::E* __restrict__ out) {
+  using E = typename F::E;
+  __shared__ E red[kReduceThreads];
+  const uint32_t slices = kReduceThreads / cw;
+  const uint32_t slice = threadIdx.x / cw;
+  const uint32_t c = blockIdx.x * cw + threadIdx.x % cw;
+  E acc = 0;
+  if (c < cols) {
+    // eight predicated loads in flight per step
+    for (uint32_t r = slice; r < rows; r += 8 * slices) {
+      E v[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        const uint32_t rr = r + k * slices;
+        v[k] = rr < rows ? partial[(uint64_t)rr * cols + c] : (E)0;
+      }
+#pragma unroll
+      for (int k = 0; k < 8; k++) acc = F::add(acc, v[k]);
+    }
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (uint32_t h = slices >> 1; h >= 1; h >>= 1) {
+    if (slice < h) red[threadIdx.x] = F::add(red[threadIdx.x], red[threadIdx.x + h * cw]);
+    __syncthreads();
+  }
+  if (slice == 0 && c < cols) out[c] = red[threadIdx.x];
+}
+
+template <class F>
+inline int launch_reduce_rows(const typename F::E* partial, uint64_t rows, uint64_t cols,
+                              typename F::E* out, cudaStream_t stream) {
+  uint32_t cw = 1;
+  while (cw < 32 && cw < cols) cw <<= 1;
+  const unsigned blocks = (unsigned)((cols + cw - 1) / cw);
+  reduce_rows_kernel<F><<<blocks, kReduceThreads, 0, stream>>>(partial, (uint32_t)rows, (uint32_t)cols,
+                                                               cw, out);
+  OMR_CUDA_TRY(cudaGetLastError());
+  return OMR_NTT_OK;
+}
+
+template <class F, int LOGT>
+inline int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void* out,
+                           cudaStream_t stream) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int T = 1 << LOGT;
+  constexpr int C = prefix_cols<F, LOGT>();
+  constexpr int NT = prefix_threads<F, LOGT>();
+  constexpr size_t smem = (size_t)T * C * sizeof(E);
+  auto kern = prefix_decomp_kernel<F, LOGT>;
+  static std::atomic<int> occ_cache[64];
+  int dev = 0;
+  OMR_CUDA_TRY(cudaGetDevice(&dev));
+  int occ = occ_cache[dev & 63].load();
+  if (occ == 0) {
+    if (smem > 48 * 1024)
+      OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
+    occ_cache[dev & 63] = occ < 1 ? 1 : occ;
+    occ = occ_cache[dev & 63];
+  }
+  RootTables rt;
+  int rc = get_root_tables(F::ID, &rt);
+  if (rc) return rc;
+  PassArgs<F> a{};
+  a.in = static_cast<const E*>(in);
+  a.L_lo = (uint32_t)(d->n >> LOGT);  // columns r
+  a.L_m = 1;
+  a.L_b = 1;
+  a.is_lo = 1;
+  a.es_in = (uint32_t)(d->n >> LOGT);
+  a.roots = static_cast<const Tw*>(rt.fwd);
+  a.roots_stride = 1u << (kMaxLogT - LOGT);
+  a.tw_lo = static_cast<const E*>(d->tw_lo_f);
+  a.tw_hi = static_cast<const Tw*>(d->tw_hi_f);
+  a.tw_scale = 1;
+  a.tw_mask = (uint32_t)(d->n - 1);
+  a.tw_line_mul_m = 0;
+  const uint32_t groups = (a.L_lo + C - 1) / C;
+  uint32_t grid = (uint32_t)device_sm_count(dev) * (uint32_t)occ;
+  if (grid > groups) grid = groups;
+  void* part = nullptr;
+  rc = domain_scratch(d, stream, (size_t)grid * m * sizeof(E), &part, 1);
+  if (rc) return rc;
+  kern<<<grid, NT, smem, stream>>>(a, m, static_cast<E*>(part));
+  OMR_CUDA_TRY(cudaGetLastError());
+  return launch_reduce_rows<F>(static_cast<const E*>(part), grid, m, static_cast<E*>(out), stream);
+}
+
+template <class F>
+int launch_prefix(omr_ntt_domain_s* d, uint32_t m, int logt, const void* in, void* out,
+                         cudaStream_t stream) {
+  if (logt <= 0) {
+    logt = 0;
+    while ((1u << logt) < m) logt++;
+    if (logt == 0) logt = 1;
+  }
+  if ((1u << logt) < m || (uint32_t)logt > d->log_n) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "decomposition line shorter than the prefix");
+  switch (logt) {
+    case 1: return launch_prefix_t<F, 1>(d, m, in, out, stream);
+    case 2: return launch_prefix_t<F, 2>(d, m, in, out, stream);
+    case 3: return launch_prefix_t<F, 3>(d, m, in, out, stream);
+    case 4: return launch_prefix_t<F, 4>(d, m, in, out, stream);
+    case 5: return launch_prefix_t<F, 5>(d, m, in, out, stream);
+    case 6: return launch_prefix_t<F, 6>(d, m, in, out, stream);
+    case 7: return launch_prefix_t<F, 7>(d, m, in, out, stream);
+    case 8: return launch_prefix_t<F, 8>(d, m, in, out, stream);
+    case 9: return launch_prefix_t<F, 9>(d, m, in, out, stream);
+    case 10: return launch_prefix_t<F, 10>(d, m, in, out, stream);
+    case 11: return launch_prefix_t<F, 11>(d, m, in, out, stream);
+    case 12: return launch_prefix_t<F, 12>(d, m, in, out, stream);
+  }
+  return fail(OMR_NTT_ERR_SIZE, "prefix decomposition needs m <= 4096");
+}
+
+extern template int launch_prefix<BabyBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
+extern template int launch_prefix<Goldilocks>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
+extern template int launch_prefix<KoalaBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
+extern template int launch_prefix<TeddyBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
+
+}  // namespace omr

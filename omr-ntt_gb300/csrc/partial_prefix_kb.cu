@@ -1,0 +1,7 @@
+// partial_prefix_kb.cu -- KoalaBear pruned prefix kernels (one translation unit
+// per field: parallel compiles).
+#include "partial_prefix.cuh"
+
+namespace omr {
+template int launch_prefix<KoalaBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
+}  // namespace omr
