@@ -270,14 +270,15 @@ int default_plan(int field, uint32_t log_n, uint64_t batch) {
   return planned_full_plan(field, log_n, batch);
 }
 
-static std::string plan_name(const PlanShape& s) {
+static std::string plan_name(int field, const PlanShape& s) {
   if (s.split.empty()) return "identity";
+  const int v = s.variant == 0 ? 0 : effective_variant(field, MODE_COL, kMaxLogT, s.variant);
   std::string n = s.split.size() == 1 ? "stockham-tile " : "four-step ";
   for (size_t i = 0; i < s.split.size(); i++) {
     if (i) n += "x";
     n += std::to_string(1 << s.split[i]);
   }
-  if (s.split.size() > 1) n += s.variant == 0 ? " tile" : (s.variant == 1 ? " tma2buf" : " tma2cta");
+  if (s.split.size() > 1) n += v == 0 ? " tile" : (v == 1 ? " tma2buf" : " tma2cta");
   return n;
 }
 
@@ -573,7 +574,7 @@ int omr_ntt_plan_describe(int field, uint32_t log_n, int plan, char* buf, size_t
   if (cnt < 0) return cnt;
   if (plan < 0) plan = default_plan(field, log_n, 1);
   if (plan >= cnt) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "plan id out of range");
-  std::string n = plan_name(enumerate_plans(log_n)[plan]);
+  std::string n = plan_name(field, enumerate_plans(log_n)[plan]);
   if (buf && cap) {
     std::strncpy(buf, n.c_str(), cap - 1);
     buf[cap - 1] = 0;

@@ -51,16 +51,23 @@ int launch_pass_logt(int logT, const PassArgs<F>& a, uint64_t blocks, cudaStream
 }
 
 // Plan variants: 0 = ntt_tile_pass (32-byte line groups, one tile per CTA);
-// 1, 2 = ntt_tile_pass_tma (persistent, TMA-fed, two thread counts), compiled
-// for the headline fields at 256..4096-point lines.
+// 1, 2 = ntt_tile_pass_tma at 256..4096-point lines, 1 double-buffered (one
+// CTA per SM), 2 two CTAs per SM.  BabyBear and Goldilocks compile both; to
+// keep the build short KoalaBear compiles variant 2 only (its arithmetic is
+// BabyBear's) and TeddyBear variant 1 only (Montgomery products need more
+// registers than two 512-thread CTAs leave); the other variant maps onto it.
+constexpr int tma_variant_mask(int field) {  // bit v-1 set: variant v compiled
+  return (field == BABYBEAR || field == GOLDILOCKS) ? 3 : (field == KOALABEAR ? 2 : 1);
+}
 template <class F>
 constexpr bool has_tma_pass() {
-  return F::ID == BABYBEAR || F::ID == GOLDILOCKS;
+  return true;
 }
 inline int effective_variant(int field, int mode, int logT, int variant) {
   if (variant <= 0 || mode == MODE_LINE || logT < 8) return 0;
-  if (field != BABYBEAR && field != GOLDILOCKS) return 0;
-  return variant > 2 ? 2 : variant;
+  int v = variant > 2 ? 2 : variant;
+  if (!((tma_variant_mask(field) >> (v - 1)) & 1)) v = 3 - v;
+  return v;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
@@ -156,6 +163,14 @@ int launch_tma_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
 // Defined here, instantiated once per (field, mode, direction) in
 // pass_<field>_<mode>_<dir>.cu; the extern declarations below stop every
 // other translation unit from instantiating the kernels again.
+template <class F, int LOGT, int MODE, bool INV, int NBUF>
+int launch_tma_compiled(const PassArgs<F>& a, int* err, cudaStream_t s) {
+  if constexpr ((tma_variant_mask(F::ID) >> (NBUF == 2 ? 0 : 1)) & 1)
+    return launch_tma_t<F, LOGT, MODE, INV, NBUF>(a, err, s);
+  else
+    return 1;  // not compiled for this field: plain tile pass
+}
+
 template <class F, int MODE, bool INV>
 int launch_pass_dir(int logT, int variant, const PassArgs<F>& a, uint64_t blocks, int* err,
                     cudaStream_t s) {
@@ -163,16 +178,16 @@ int launch_pass_dir(int logT, int variant, const PassArgs<F>& a, uint64_t blocks
     if (variant >= 1) {
       int rc = 1;
       switch (logT * 4 + variant) {
-        case 8 * 4 + 1: rc = launch_tma_t<F, 8, MODE, INV, 2>(a, err, s); break;
-        case 9 * 4 + 1: rc = launch_tma_t<F, 9, MODE, INV, 2>(a, err, s); break;
-        case 10 * 4 + 1: rc = launch_tma_t<F, 10, MODE, INV, 2>(a, err, s); break;
-        case 11 * 4 + 1: rc = launch_tma_t<F, 11, MODE, INV, 2>(a, err, s); break;
-        case 12 * 4 + 1: rc = launch_tma_t<F, 12, MODE, INV, 2>(a, err, s); break;
-        case 8 * 4 + 2: rc = launch_tma_t<F, 8, MODE, INV, 1>(a, err, s); break;
-        case 9 * 4 + 2: rc = launch_tma_t<F, 9, MODE, INV, 1>(a, err, s); break;
-        case 10 * 4 + 2: rc = launch_tma_t<F, 10, MODE, INV, 1>(a, err, s); break;
-        case 11 * 4 + 2: rc = launch_tma_t<F, 11, MODE, INV, 1>(a, err, s); break;
-        case 12 * 4 + 2: rc = launch_tma_t<F, 12, MODE, INV, 1>(a, err, s); break;
+        case 8 * 4 + 1: rc = launch_tma_compiled<F, 8, MODE, INV, 2>(a, err, s); break;
+        case 9 * 4 + 1: rc = launch_tma_compiled<F, 9, MODE, INV, 2>(a, err, s); break;
+        case 10 * 4 + 1: rc = launch_tma_compiled<F, 10, MODE, INV, 2>(a, err, s); break;
+        case 11 * 4 + 1: rc = launch_tma_compiled<F, 11, MODE, INV, 2>(a, err, s); break;
+        case 12 * 4 + 1: rc = launch_tma_compiled<F, 12, MODE, INV, 2>(a, err, s); break;
+        case 8 * 4 + 2: rc = launch_tma_compiled<F, 8, MODE, INV, 1>(a, err, s); break;
+        case 9 * 4 + 2: rc = launch_tma_compiled<F, 9, MODE, INV, 1>(a, err, s); break;
+        case 10 * 4 + 2: rc = launch_tma_compiled<F, 10, MODE, INV, 1>(a, err, s); break;
+        case 11 * 4 + 2: rc = launch_tma_compiled<F, 11, MODE, INV, 1>(a, err, s); break;
+        case 12 * 4 + 2: rc = launch_tma_compiled<F, 12, MODE, INV, 1>(a, err, s); break;
         default: break;
       }
       if (rc != 1) return rc;

@@ -145,16 +145,18 @@ int mlp_select_class(int field, uint32_t log_n, uint64_t batch, int pattern, uin
 
 static bool g_use_mlp = false;
 
-// The network is trusted only inside the domain it was trained on: log2 n in
-// [10, 24], batch <= 512, batch * n <= 2^26 words.  Outside it the planner
-// falls back to the built-in rule (a 2^27 transform is not extrapolated).
+// The network is trusted only inside the domain it was trained on: BabyBear
+// or Goldilocks, log2 n in [10, 24], batch <= 512, batch * n <= 2^26 words.
+// Outside it the planner falls back to the built-in rule (a 2^27 transform,
+// or a KoalaBear one, is not extrapolated).
 constexpr uint32_t kMlpMinLogN = 10, kMlpMaxLogN = 24;
 constexpr uint64_t kMlpMaxBatch = 512, kMlpMaxWords = 1ull << 26;
 
 static bool mlp_choice(int field, uint32_t log_n, uint64_t batch, int pattern, uint64_t count,
                        Cand* out) {
   if (!g_use_mlp) return false;
-  if (log_n < kMlpMinLogN || log_n > kMlpMaxLogN || batch > kMlpMaxBatch ||
+  if ((field != BABYBEAR && field != GOLDILOCKS) || log_n < kMlpMinLogN || log_n > kMlpMaxLogN ||
+      batch > kMlpMaxBatch ||
       (batch << log_n) > kMlpMaxWords)
     return false;
   bool app[kNumClasses];
@@ -227,12 +229,13 @@ static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   (void)batch;
   const auto plans = enumerate_plans(log_n);
   if (plans.size() <= 1 || plans[0].split.size() < 2) return 0;
-  if (field != BABYBEAR && field != GOLDILOCKS) return 0;
   size_t nsplit = 0;
   for (auto& p : plans)
     if (p.variant == 0) nsplit++;
-  // BabyBear: variant 2 (two CTAs per SM); Goldilocks: variant 1 (double-buffered)
-  const int cand = (int)nsplit * (field == BABYBEAR ? 2 : 1);  // first (balanced) split
+  // 31-bit fields: variant 2 (two CTAs per SM at <= 64 registers); Goldilocks
+  // and TeddyBear (wider arithmetic): variant 1 (double-buffered)
+  const bool narrow = field == BABYBEAR || field == KOALABEAR;
+  const int cand = (int)nsplit * (narrow ? 2 : 1);  // first (balanced) split
   return cand < (int)plans.size() ? cand : 0;
 }
 

@@ -70,6 +70,23 @@ def test_forward_inverse_large(oracle, field, log_n):
 
 
 @pytest.mark.parametrize("field", [KoalaBear, TeddyBear], ids=lambda f: f.name)
+@pytest.mark.parametrize("log_n", [16, 20, 24])
+def test_other_fields_every_plan(oracle, field, log_n):
+    """KoalaBear and TeddyBear on every plan, the TMA tile passes included."""
+    n = 1 << log_n
+    d = NttDomain(field, n)
+    x = gen_input_seeded(field, n, 5 + log_n)
+    exp = oracle.forward(field.id, x)
+    xd = to_dev(x)
+    for plan in range(omr_ntt.plan_count(field, log_n)):
+        yd = xd.clone()
+        omr_ntt.forward(d, yd, plan=plan)
+        assert np.array_equal(to_host(yd, field.dtype), exp), plan
+        omr_ntt.inverse(d, yd, plan=plan)
+        assert np.array_equal(to_host(yd, field.dtype), x), plan
+
+
+@pytest.mark.parametrize("field", [KoalaBear, TeddyBear], ids=lambda f: f.name)
 def test_other_fields_large(oracle, field):
     for log_n in (17, 21):
         n = 1 << log_n
