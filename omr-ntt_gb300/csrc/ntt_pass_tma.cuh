@@ -324,9 +324,11 @@ __global__ void __launch_bounds__(NT, 3 - NBUF)
   using E = typename F::E;
   using Tw = typename F::Tw;
   constexpr size_t BW = tma_buf_words<F, LOGT, C>();
-  // declared with the same alignment as the other kernels' dynamic shared
-  // memory; the buffers are aligned to 128 bytes below
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // the dynamic shared memory under its own name (every extern __shared__
+  // array starts at the same address) so that its 128-byte alignment does not
+  // conflict with the 16-byte declarations of the other kernels in a unit
+  extern __shared__ __align__(128) unsigned char tma_smem_raw[];
+  unsigned char* smem_raw = tma_smem_raw;
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ int abort_flag;
   // align by pointer arithmetic on the shared array (keeps the state space)
