@@ -160,3 +160,43 @@ def test_noncanonical_check():
     x2[100] = BabyBear.p
     xd2 = to_dev(x2)
     assert _lib.lib().omr_ntt_check_canonical(d.handle, ctypes.c_void_p(xd2.data_ptr()), n, None) == -7
+
+
+def test_one_domain_shared_by_threads_on_their_own_streams(oracle):
+    """The reference's encoders are Send + Sync and a domain is shared
+    read-only; here four host threads drive one domain on four CUDA streams
+    (per-stream scratch) and every result stays bit-exact."""
+    import ctypes
+    import threading
+
+    import torch
+    from omr_ntt import _lib
+
+    f, log_n = BabyBear, 20
+    n = 1 << log_n
+    d = NttDomain(f, n)
+    xs = [gen_input_seeded(f, n, 300 + t) for t in range(4)]
+    exps = [oracle.forward(f.id, x) for x in xs]
+    errors = []
+
+    def work(t):
+        try:
+            st = torch.cuda.Stream()
+            with torch.cuda.stream(st):
+                for _ in range(5):
+                    buf = torch.from_numpy(xs[t].view(np.int32)).cuda()
+                    _lib.check(_lib.lib().omr_ntt_forward(d.handle, -1, ctypes.c_void_p(buf.data_ptr()),
+                                                          ctypes.c_void_p(buf.data_ptr()), 1,
+                                                          ctypes.c_void_p(st.cuda_stream)))
+                    st.synchronize()
+                    if not np.array_equal(buf.cpu().numpy().view(np.uint32), exps[t]):
+                        errors.append(t)
+        except Exception as e:  # surfaced below
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=work, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
