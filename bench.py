@@ -155,7 +155,7 @@ def cpu_baseline(field, log_n, seconds, steps=None):
 
 
 def cpu_config_samples(extras, partial, headline_ms, field, log_n):
-    """Each BASELINE shape timed on the host cores with the oracle's C
+    """Each benchmark shape timed on the host cores with the oracle's C
     restatement of the reference encoder the crate's benches use for it
     (ArkRadix2 at 2^16, TfheStockhamRadix8 and WinterfellFourStep at 2^24,
     WinterfellFourStep on the 64 x 2^20 batch, TransformDecomposition for
@@ -331,7 +331,7 @@ def main():
         e2e_t.append(time.perf_counter() - t0)
     e2e_val = n * world * len(e2e_t) / sum(e2e_t) / 1e9
 
-    # ---- extras: other BASELINE config-2 shapes (a few steps each)
+    # ---- extras: the other full-transform shapes (2^16..2^27, batch 64 x 2^20; a few steps each)
     extras = {}
     if not args.no_extras:
         def timed(fn, reps=5):

@@ -1,4 +1,4 @@
-"""Partial-output transforms on the GPU (BASELINE config 3): N = 2^22,
+"""Partial-output transforms on the GPU: N = 2^22,
 s in {2^4, 2^6, ..., 2^16}, contiguous / strided / random index sets, both
 fields, bit-exact against the matching entries of the oracle's full
 transform."""
