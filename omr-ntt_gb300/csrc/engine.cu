@@ -167,6 +167,9 @@ std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
       if (v > 0 && s.size() == 1) continue;  // single-pass plans have one kernel
       out.push_back(PlanShape{s, v});
     }
+  // 2^13..2^16: the balanced two-pass plan as one launch on an 8-CTA cluster
+  // (appended, so the other plans keep their ids)
+  if (log_n >= 13 && log_n <= 16) out.push_back(PlanShape{splits[0], kClusterVariant});
   return out;
 }
 
@@ -278,6 +281,7 @@ static std::string plan_name(int field, const PlanShape& s) {
     if (i) n += "x";
     n += std::to_string(1 << s.split[i]);
   }
+  if (s.variant == kClusterVariant) return n + " cluster";
   if (s.split.size() > 1) n += v == 0 ? " tile" : (v == 1 ? " tma2buf" : " tma2cta");
   return n;
 }
@@ -377,6 +381,10 @@ int run_transform(omr_ntt_domain_s* d, int plan, bool inverse, const void* in, v
     return OMR_NTT_OK;
   }
   std::vector<PassDesc> ps = build_passes(d->log_n, batch, d->plans[plan]);
+  if (d->plans[plan].variant == kClusterVariant) {
+    int rc = launch_cluster_transform(d, ps, inverse, in, out, batch, stream);
+    if (rc <= 0) return rc;  // launched, or an error; 1: run the passes below
+  }
   void* scratch = nullptr;
   if (ps.size() > 1) {
     int rc = domain_scratch(d, stream, bytes, &scratch);

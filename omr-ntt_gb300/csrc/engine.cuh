@@ -49,7 +49,7 @@ struct PassDesc {
 // A plan = a split of log N into pass sizes (each 1..12, at most 3 passes).
 struct PlanShape {
   std::vector<int> split;  // log2 of each pass's line length, first pass first
-  int variant = 0;         // pass kernel variant of the multi-pass plans
+  int variant = 0;         // pass kernel variant of the multi-pass plans (3: one cluster launch)
 };
 
 std::vector<PlanShape> enumerate_plans(uint32_t log_n);
@@ -58,6 +58,12 @@ int default_plan(int field, uint32_t log_n, uint64_t batch);
 // The planner's full-transform plan: planner database, learned selector, else
 // built-in heuristic (tuner.cu).
 int planned_full_plan(int field, uint32_t log_n, uint64_t batch);
+// One-launch transform of a two-pass plan on an 8-CTA cluster (ntt_cluster.cu):
+// 0 launched, 1 not available for this shape (run the passes), < 0 error.
+int launch_cluster_transform(const omr_ntt_domain_s* d, const std::vector<PassDesc>& ps,
+                             bool inverse, const void* in, void* out, uint64_t batch,
+                             cudaStream_t stream);
+constexpr int kClusterVariant = 3;  // PlanShape::variant of the cluster plans
 // The planner's partial strategy (1 if the database or the learned selector has one).
 int planned_partial(int field, uint32_t log_n, int pattern, uint64_t count, int* strategy,
                     int* param);

@@ -212,15 +212,17 @@ OMR_EXTERN_PASS_MODES(KoalaBear)
 OMR_EXTERN_PASS_MODES(TeddyBear)
 
 
+// Kernel arguments of one pass descriptor.
 template <class F>
-int launch_pass(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, const void* in,
-                void* out, bool last, cudaStream_t stream) {
+int make_pass_args(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, const void* in,
+                   void* out, bool last, PassArgs<F>* out_args) {
   using E = typename F::E;
   using Tw = typename F::Tw;
   RootTables rt;
   int rc = get_root_tables(F::ID, &rt);
   if (rc) return rc;
-  PassArgs<F> a{};
+  PassArgs<F>& a = *out_args;
+  a = PassArgs<F>{};
   a.in = static_cast<const E*>(in);
   a.out = static_cast<E*>(out);
   a.L_lo = p.L_lo;
@@ -247,8 +249,17 @@ int launch_pass(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, cons
   a.tw_line_mul_m = p.tw_line_mul_m;
   a.has_scale = (inverse && last) ? 1 : 0;
   a.scale = F::make_tw(d->n_inv);
-  const int variant = effective_variant(F::ID, p.mode, p.logT, p.variant);
   a.L_b = p.L_b;
+  return OMR_NTT_OK;
+}
+
+template <class F>
+int launch_pass(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, const void* in,
+                void* out, bool last, cudaStream_t stream) {
+  PassArgs<F> a;
+  int rc = make_pass_args<F>(d, p, inverse, in, out, last, &a);
+  if (rc) return rc;
+  const int variant = effective_variant(F::ID, p.mode, p.logT, p.variant);
   const int C = tile_cols<F, 0>();
   const uint64_t blocks = p.L_b * (uint64_t)p.L_m * (uint64_t)((p.L_lo + C - 1) / C);
   switch (p.mode) {

@@ -65,7 +65,9 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
 // A fixed, size-independent plan vocabulary for the learned planner:
 //   0..11   full transform: split kind x kernel variant 0..2 (class = 4 variant + kind);
 //           kind 0: balanced split with the fewest passes, 1: its reverse,
-//           2: balanced with one more pass, 3: large-first (4096, ..., 4096, remainder)
+//           2: balanced with one more pass, 3: large-first (4096, ..., 4096, remainder);
+//           class 3 itself (plain tile pass, large-first: never the fastest
+//           on GB300) stands for the one-launch cluster plan of 2^13..2^16
 //   12..15  prefix decomposition with line length next_pow2(count) << j, j = 0..3
 //   16..27  strided fold, then the count-point transform with full class (c - 16)
 //   28..39  full transform with full class (c - 28), then gather
@@ -75,6 +77,11 @@ constexpr int kNumClasses = 40;
 static int full_class_plan(uint32_t log_n, int fc) {
   const auto plans = enumerate_plans(log_n);
   if (log_n == 0) return fc == 0 ? 0 : -1;
+  if (fc == 3) {
+    for (int i = 0; i < (int)plans.size(); i++)
+      if (plans[i].variant == kClusterVariant) return i;
+    return -1;
+  }
   const int variant = fc / 4, kind = fc % 4;
   const int pmin = std::max<int>(1, (int)((log_n + kMaxLogT - 1) / kMaxLogT));
   const int P = pmin + (kind == 2 ? 1 : 0);
@@ -226,9 +233,13 @@ static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, ui
 // Built-in heuristic (measured on GB300): the two-buffer TMA pass for the
 // headline fields' balanced split, the tile pass otherwise.
 static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
-  (void)batch;
   const auto plans = enumerate_plans(log_n);
   if (plans.size() <= 1 || plans[0].split.size() < 2) return 0;
+  // the one-launch cluster plan wins where latency dominates: up to 2^14, or
+  // batches of 8 and more (one cluster per transform)
+  if (log_n <= 14 || batch >= 8)
+    for (int i = 0; i < (int)plans.size(); i++)
+      if (plans[i].variant == kClusterVariant) return i;
   size_t nsplit = 0;
   for (auto& p : plans)
     if (p.variant == 0) nsplit++;

@@ -199,16 +199,22 @@ def heuristic_class(p) -> int:
     rule): tuned TMA kernel on the balanced split for the headline fields,
     decomposition for prefixes <= 4096, fold for strided sets, else gather."""
     tma_cls = {0: 8, 1: 4}  # BabyBear: two CTAs per SM; Goldilocks: double-buffered
-    full_cls = tma_cls[p["field"]] if (p["log_n"] > 12 and p["field"] in (0, 1)) else 0
+
+    def full_class(log_n, batch):
+        if 13 <= log_n <= 16 and (log_n <= 14 or batch >= 8):
+            return 3  # the one-launch cluster plan
+        return tma_cls[p["field"]] if (log_n > 12 and p["field"] in (0, 1)) else 0
+
+    full_cls = full_class(p["log_n"], p["batch"])
     n, s = 1 << p["log_n"], point_count(p)
     if s >= n:
         return full_cls
     if p["pattern"] == "strided":
-        sub_full = tma_cls[p["field"]] if (p["log_s"] > 12 and p["field"] in (0, 1)) else 0
+        sub_full = full_class(p["log_s"], 1)
         return 16 + sub_full
     if p["pattern"] == "contiguous" and s <= 4096 and n // s >= 2:
         return 12
-    return 28 + full_cls
+    return 28 + full_class(p["log_n"], 1)  # the gather runs one transform at a time
 
 
 def regret(T, best, choice):

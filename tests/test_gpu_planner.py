@@ -40,6 +40,9 @@ def _cands(field, log_n, pattern, count):
     (Goldilocks, 14, 1, 2, 1),
     (KoalaBear, 12, 1, 1, 2),
     (Goldilocks, 20, 1, 16, 1),
+    (BabyBear, 16, 0, 1 << 16, 3),
+    (Goldilocks, 13, 0, 1 << 13, 2),
+    (TeddyBear, 15, 0, 1 << 15, 2),
 ], ids=str)
 def test_all_candidates_agree(oracle, field, log_n, pattern, count, batch):
     import torch
