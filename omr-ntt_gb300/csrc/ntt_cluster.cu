@@ -1,15 +1,17 @@
 // ntt_cluster.cu -- one-launch four-step transforms for 2^13 <= N <= 2^16 on
-// an 8-CTA thread-block cluster.
+// a thread-block cluster (8 CTAs up to 2^14, 16 CTAs -- a non-portable
+// cluster size GB300 allows -- at 2^15 and 2^16).
 //
 // A two-pass plan for a small N is latency bound: two launches, each a short
-// wave of tiles.  Here one cluster of kClusterCtas CTAs owns one transform
-// (N = N1 x N2; the grid holds one cluster per transform of the batch):
+// wave of tiles.  Here one cluster of CL CTAs owns one transform
+// (N = N1 x N2; the grid holds one cluster per transform of the
+// batch):
 //   1. CTA r runs the N1-point column transforms of columns
-//      [r W, (r + 1) W), W = N2 / 8, with the tile-pass rounds (first round
+//      [r W, (r + 1) W), W = N2 / CL, with the tile-pass rounds (first round
 //      straight from global memory) and leaves the four-step-twiddled results
 //      in its shared memory;
 //   2. after a cluster barrier, CTA r gathers rows [r H, (r + 1) H),
-//      H = N1 / 8, of all N2 columns from the eight tiles through
+//      H = N1 / CL, of all N2 columns from the CL tiles through
 //      distributed shared memory (the peers' tiles mapped into its address
 //      space) into a second shared-memory tile;
 //   3. it runs the N2-point row transforms and writes X[k1 + N1 k2] straight
@@ -26,8 +28,8 @@ namespace omr {
 
 namespace cg = cooperative_groups;
 
-constexpr int kClusterCtas = 8;
 constexpr int kClusterThreads = 256;
+constexpr int cluster_ctas(int log_n) { return log_n <= 14 ? 8 : 16; }
 
 template <class F, int LOG1, int W, bool INV, int I>
 OMR_D void cluster_columns(const PassArgs<F>& a, typename F::E* s, const typename F::E* gin,
@@ -43,18 +45,19 @@ OMR_D void cluster_columns(const PassArgs<F>& a, typename F::E* s, const typenam
 }
 
 template <class F, int LOG1, int LOG2, bool INV>
-__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads)
+__global__ void __launch_bounds__(kClusterThreads)
     ntt_cluster_kernel(const PassArgs<F> a, const PassArgs<F> b) {
   using E = typename F::E;
+  constexpr int CL = cluster_ctas(LOG1 + LOG2);
   constexpr int N1 = 1 << LOG1, N2 = 1 << LOG2;
-  constexpr int W = N2 / kClusterCtas;  // pass-1 columns per CTA
-  constexpr int H = N1 / kClusterCtas;  // pass-2 rows per CTA
+  constexpr int W = N2 / CL;  // pass-1 columns per CTA
+  constexpr int H = N1 / CL;  // pass-2 rows per CTA
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E* ta = reinterpret_cast<E*>(smem_raw);  // [N1][W], tile_idx<F, W>
   E* tb = ta + N1 * W;                     // [N2][H], tile_idx<F, H>
   cg::cluster_group cluster = cg::this_cluster();
   const uint32_t r = cluster.block_rank();
-  const uint64_t t = blockIdx.x / kClusterCtas;  // transform of the batch
+  const uint64_t t = blockIdx.x / CL;  // transform of the batch
 
   cluster_columns<F, LOG1, W, INV, 0>(a, ta, a.in + t * a.is_b + r * W, r * W);
   cluster.sync();  // every pass-1 tile complete and visible to the cluster
@@ -73,18 +76,56 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterT
 template <class F, int LOG1, int LOG2, bool INV>
 static int launch_cluster_t(const PassArgs<F>& a, const PassArgs<F>& b, uint64_t batch,
                             cudaStream_t stream) {
-  constexpr size_t smem = (size_t)2 * ((size_t)1 << (LOG1 + LOG2)) / kClusterCtas * F::WORD;
+  constexpr int CL = cluster_ctas(LOG1 + LOG2);
+  constexpr size_t smem = (size_t)2 * ((size_t)1 << (LOG1 + LOG2)) / CL * F::WORD;
   auto kern = ntt_cluster_kernel<F, LOG1, LOG2, INV>;
-  static std::atomic<int> attr_set[64];
+  static std::atomic<int> attr_set[64];  // per device: 1 attributes set, -1 not launchable
   int dev = 0;
   OMR_CUDA_TRY(cudaGetDevice(&dev));
-  if (smem > 48 * 1024 && !attr_set[dev & 63].load()) {
-    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set[dev & 63] = 1;
+  int st = attr_set[dev & 63].load();
+  if (st < 0) return 1;
+  if (st == 0) {
+    bool ok = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+              cudaSuccess;
+    if (ok && CL > 8)
+      ok = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+    if (ok) {
+      // the cluster must fit on the device at all
+      cudaLaunchConfig_t qc = {};
+      cudaLaunchAttribute qa[1];
+      qa[0].id = cudaLaunchAttributeClusterDimension;
+      qa[0].val.clusterDim.x = CL;
+      qa[0].val.clusterDim.y = 1;
+      qa[0].val.clusterDim.z = 1;
+      qc.gridDim = dim3(CL);
+      qc.blockDim = dim3(kClusterThreads);
+      qc.dynamicSmemBytes = smem;
+      qc.attrs = qa;
+      qc.numAttrs = 1;
+      int clusters = 0;
+      ok = cudaOccupancyMaxActiveClusters(&clusters, kern, &qc) == cudaSuccess && clusters > 0;
+    }
+    cudaGetLastError();  // a refused attribute or query is not an error of this call
+    attr_set[dev & 63] = ok ? 1 : -1;
+    if (!ok) return 1;
   }
-  if (batch * kClusterCtas > 0x7fffffffull) return 1;
-  kern<<<(unsigned)(batch * kClusterCtas), kClusterThreads, smem, stream>>>(a, b);
-  if (cudaGetLastError() != cudaSuccess) return 1;  // not launchable here: caller runs the passes
+  if (batch * CL > 0x7fffffffull) return 1;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)(batch * CL));
+  cfg.blockDim = dim3(kClusterThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, kern, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;  // not launchable here: the caller runs the passes
+  }
   return OMR_NTT_OK;
 }
 
