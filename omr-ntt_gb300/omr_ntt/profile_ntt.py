@@ -6,6 +6,7 @@ log N = 27: two warm-up calls, then timed calls on seed 42).
     python -m omr_ntt.profile_ntt --mode forward --field BabyBear --log-n 24 --plan -1 --iters 2
     python -m omr_ntt.profile_ntt --mode partial --log-n 22 --pattern 1 --s 16
     python -m omr_ntt.profile_ntt --mode batch --requests 512   # mixed batch, graph launch
+    python -m omr_ntt.profile_ntt --mode forward --log-n 16 --batch 64 --plan 15
 
 Runs on device buffers through the C ABI with no host copies in the loop, so
 that a profiler sees only the engine's kernels (plus one buffer fill).
@@ -31,6 +32,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--iters", type=int, default=5)
     ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--batch", type=int, default=1, help="transforms per forward/inverse call")
     a = ap.parse_args(argv)
 
     import torch
@@ -45,7 +47,8 @@ def main(argv=None):
     d = NttDomain(fld, n)
     dt = torch.int32 if fld.word_bytes == 4 else torch.int64
     g = torch.Generator(device="cuda").manual_seed(42)
-    x = torch.randint(0, 1 << 30, (n,), dtype=dt, device="cuda", generator=g)
+    bt = a.batch if a.mode in ("forward", "inverse") else 1
+    x = torch.randint(0, 1 << 30, (n * bt,), dtype=dt, device="cuda", generator=g)
     out = torch.empty(max(a.s, 1) if a.mode == "partial" else n, dtype=dt, device="cuda")
     L = _lib.lib()
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -67,9 +70,9 @@ def main(argv=None):
             e = cls(a.s) if cls.ID in (2, 7, 8) else cls()
             _lib.check(L.omr_ntt_encode(d.handle, e.ID, e.s, p, 1, st))
         elif a.mode == "forward":
-            _lib.check(L.omr_ntt_forward(d.handle, a.plan, p, p, 1, st))
+            _lib.check(L.omr_ntt_forward(d.handle, a.plan, p, p, bt, st))
         elif a.mode == "inverse":
-            _lib.check(L.omr_ntt_inverse(d.handle, a.plan, p, p, 1, st))
+            _lib.check(L.omr_ntt_inverse(d.handle, a.plan, p, p, bt, st))
         else:
             ip = ctypes.c_void_p(idx.data_ptr()) if idx is not None else None
             _lib.check(L.omr_ntt_partial(d.handle, a.pattern, a.s, ip, p, ctypes.c_void_p(out.data_ptr()), st))
