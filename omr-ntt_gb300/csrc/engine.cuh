@@ -100,6 +100,7 @@ struct omr_ntt_domain_s {
   int* err = nullptr;  // device error word raised by bounded waits (OMR_NTT_ERR_TIMEOUT)
   std::mutex mu;       // guards `scratch`
   std::mutex host_mu;  // serialises the synchronous host-buffer calls
+  cudaStream_t host_streams[3] = {nullptr, nullptr, nullptr};  // copy-in, compute, copy-out
   std::map<std::pair<void*, int>, omr::Scratch> scratch;  // keyed by (stream, slot)
   std::vector<omr::PlanShape> plans;
   std::map<uint32_t, omr_ntt_domain_s*> subs;  // smaller domains (same field) for partial paths

@@ -200,3 +200,18 @@ def test_one_domain_shared_by_threads_on_their_own_streams(oracle):
     for th in threads:
         th.join()
     assert not errors, errors
+
+
+@pytest.mark.parametrize("field,log_n,batch", [(BabyBear, 16, 8), (BabyBear, 20, 5), (Goldilocks, 18, 3),
+                                               (TeddyBear, 12, 2)], ids=str)
+def test_host_buffer_batches_pipelined(oracle, field, log_n, batch):
+    """Host-buffer batches run chunk by chunk through two device buffers on
+    three streams (copy in / transform / copy out); the words match the
+    oracle, forward and back."""
+    n = 1 << log_n
+    d = NttDomain(field, n)
+    x = gen_input_seeded(field, n * batch, 11 + log_n)
+    exp = oracle.forward(field.id, x, batch=batch)
+    got = omr_ntt.forward(d, x, batch=batch)
+    assert np.array_equal(got, exp)
+    assert np.array_equal(omr_ntt.inverse(d, got, batch=batch), x)
