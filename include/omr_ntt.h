@@ -5,11 +5,11 @@
  * The reference crate's interface (Rust) is
  *
  *   pub struct NttDomain<F> { N, log_N, omega, twiddles, bitrev_twiddles }
- *                                                   (src/encoder.rs:28-38)
- *   NttDomain::<F>::new(N)                          (src/encoder.rs:42-70)
+ *                                                   (src/encoder.rs:9-19)
+ *   NttDomain::<F>::new(N)                          (src/encoder.rs:23-51)
  *   pub trait NttEncoder<F>: Send + Sync {
  *       fn ntt(&self, buf: &mut [F], domain: &NttDomain<F>);
- *       fn name(&self) -> &str;                     (src/encoder.rs:89-93)
+ *       fn name(&self) -> &str;                     (src/encoder.rs:70-74)
  *   }
  *   encoders::all(log_n) / encoders::all_partial(s) (src/encoders/mod.rs:32-54)
  *
@@ -18,7 +18,7 @@
  * BabyBear, KoalaBear and TeddyBear, uint64_t for Goldilocks (a Rust shim
  * converts ark-ff's Montgomery-form Fp to and from canonical integers).
  *
- * Errors: the reference panics through assert! (src/encoder.rs:43-51,
+ * Errors: the reference panics through assert! (src/encoder.rs:24-32,
  * src/encoders/lambdaworks_radix4.rs:17-21, tfhe_stockham_radix8.rs:17-21,
  * transform_decomposition.rs:28); every function here returns an
  * omr_ntt_status instead and leaves the caller's buffers untouched on a
@@ -91,7 +91,7 @@ typedef struct omr_ntt_domain_s *omr_ntt_domain_t;
 
 /* ---------------------------------------------------------------- domain */
 
-/* NttDomain::<F>::new(N) (src/encoder.rs:42-70) with N = 2^log_n.  Builds the
+/* NttDomain::<F>::new(N) (src/encoder.rs:23-51) with N = 2^log_n.  Builds the
  * device twiddle tables on the current CUDA device (setup, untimed in the
  * reference's benches: benches/ntt_bench_n.rs:10). */
 int omr_ntt_domain_create(int field, uint32_t log_n, omr_ntt_domain_t *out);
@@ -104,25 +104,25 @@ int omr_ntt_domain_destroy(omr_ntt_domain_t d);
  * the word is then cleared).  Host-buffer calls check it themselves. */
 int omr_ntt_domain_check(omr_ntt_domain_t d, void *stream);
 
-/* NttDomain fields N, log_N, omega (src/encoder.rs:30-33); omega canonical. */
+/* NttDomain fields N, log_N, omega (src/encoder.rs:11-14); omega canonical. */
 int omr_ntt_domain_info(omr_ntt_domain_t d, int *field, uint64_t *n, uint32_t *log_n,
                         uint64_t *omega);
 
 /* NttDomain::twiddles (bitrev == 0: omega^k, k < N) or bitrev_twiddles
- * (bitrev != 0: omega^bitrev(i, log_N - 1), i < N/2) (src/encoder.rs:34-37,
- * :56-62), copied to host memory `out` of N (resp. N/2) words. */
+ * (bitrev != 0: omega^bitrev(i, log_N - 1), i < N/2) (src/encoder.rs:15-18,
+ * :37-43), copied to host memory `out` of N (resp. N/2) words. */
 int omr_ntt_domain_twiddles(omr_ntt_domain_t d, int bitrev, void *out);
 
 /* ---------------------------------------------------------------- encoders */
 
-/* NttEncoder::name (src/encoder.rs:92): the reference encoder's name, or NULL. */
+/* NttEncoder::name (src/encoder.rs:73): the reference encoder's name, or NULL. */
 const char *omr_ntt_encoder_name(int encoder);
 
 /* Whether `encoder` accepts log_n (radix-4: even; radix-8: divisible by 3),
- * mirroring the reference's registry filter (src/encoders/mod.rs:41-46). */
+ * mirroring the reference's registry filter (src/encoders/mod.rs:39-44). */
 int omr_ntt_encoder_supports(int encoder, uint32_t log_n);
 
-/* NttEncoder::ntt(&self, buf, domain) (src/encoder.rs:90) on a device buffer:
+/* NttEncoder::ntt(&self, buf, domain) (src/encoder.rs:71) on a device buffer:
  * in place on `batch` transforms of N words stored back to back.  Partial
  * encoders (DftPartial, TransformDecomposition, TransformDecompositionV2) use
  * `s` and write only buf[..min(2s, N)] of each transform, as the reference

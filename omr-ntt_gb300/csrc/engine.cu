@@ -418,7 +418,7 @@ int omr_ntt_domain_create(int field, uint32_t log_n, omr_ntt_domain_t* out) {
   if (!out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null output handle");
   *out = nullptr;
   if (!valid_field(field)) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown field id");
-  // NttDomain::new asserts log2 N <= TWO_ADICITY (src/encoder.rs:47-51)
+  // NttDomain::new asserts log2 N <= TWO_ADICITY (src/encoder.rs:28-32)
   if ((int)log_n > two_adicity(field))
     return fail(OMR_NTT_ERR_SIZE, "N=2^" + std::to_string(log_n) +
                                       " requires log2(N) <= TWO_ADICITY=" +

@@ -18,7 +18,7 @@
 //   * Goldilocks: 64x64->128 product and the 2^64 = 2^32 - 1, 2^96 = -1 (mod p)
 //     folding; twiddles are plain canonical words.
 // Roots of unity follow ark-ff's convention used by NttDomain::new
-// (src/encoder.rs:53): omega_N = GEN^((p - 1) / N) for N a power of two.
+// (src/encoder.rs:34): omega_N = GEN^((p - 1) / N) for N a power of two.
 #pragma once
 #include <cstdint>
 

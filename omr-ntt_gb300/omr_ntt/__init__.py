@@ -3,9 +3,9 @@
 The names follow benbencik/omr-ntt so its tests and benches read the same:
 
     from omr_ntt import NttDomain, DefaultField, encoders
-    domain = NttDomain(DefaultField, 1 << 16)          # src/encoder.rs:42-70
+    domain = NttDomain(DefaultField, 1 << 16)          # src/encoder.rs:23-51
     for encoder in encoders.all(16):                    # src/encoders/mod.rs:32-46
-        encoder.ntt(buf, domain)                        # src/encoder.rs:89-93
+        encoder.ntt(buf, domain)                        # src/encoder.rs:70-74
 
 ``buf`` is either a NumPy array of canonical words (host; the call copies
 through the GPU and back, like the reference's in-place ``&mut [F]``) or a
@@ -49,13 +49,13 @@ def _stream_of(x, stream):
 
 
 class NttDomain:
-    """Reusable NTT parameters (src/encoder.rs:28-70): N, log_N, omega and the
+    """Reusable NTT parameters (src/encoder.rs:9-51): N, log_N, omega and the
     device twiddle tables.  ``twiddles`` / ``bitrev_twiddles`` are fetched on
     first use (as NumPy arrays)."""
 
     def __init__(self, field: Field, N: int):
         if N <= 0 or N & (N - 1):
-            # NttDomain::new asserts N.is_power_of_two() (src/encoder.rs:43)
+            # NttDomain::new asserts N.is_power_of_two() (src/encoder.rs:24)
             raise OmrNttError(-2, f"NTT size N={N} must be a power of 2")
         self.field = field
         self.N = int(N)

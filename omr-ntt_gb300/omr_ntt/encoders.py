@@ -1,7 +1,7 @@
 """The reference's encoder registry (src/encoders/mod.rs) over the GPU engine.
 
 Each class keeps the reference encoder's name, constructor and ``ntt`` /
-``name`` methods (src/encoder.rs:89-93).  All of them compute the same
+``name`` methods (src/encoder.rs:70-74).  All of them compute the same
 natural-order transform on the GPU (the id selects the plan family); the
 partial encoders write only ``buf[..min(2s, N)]`` as the reference does.
 Preconditions raise ``OmrNttError`` (status PRECONDITION) where the
@@ -20,7 +20,7 @@ TRANSFORM_DECOMPOSITION_V2, WINTERFELL_FOUR_STEP = 8, 9
 
 
 class NttEncoder:
-    """trait NttEncoder<F> (src/encoder.rs:89-93)."""
+    """trait NttEncoder<F> (src/encoder.rs:70-74)."""
 
     ID = -1
     s = 0

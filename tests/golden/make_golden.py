@@ -7,7 +7,7 @@ the definition, with arbitrary-precision Python integers and nothing else:
 
     omega_N = GEN^((p - 1) / N)            ark-ff's get_root_of_unity, as
                                            called by NttDomain::new
-                                           (src/encoder.rs:53-54)
+                                           (src/encoder.rs:34-35)
     X[k]    = sum_i x[i] omega_N^(ik)      the DFT that Dft computes
                                            (src/encoders/dft.rs:9-22)
     x[i]    = N^-1 sum_k X[k] omega_N^(-ik)
