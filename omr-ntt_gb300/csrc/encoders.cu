@@ -122,6 +122,12 @@ int omr_ntt_encode_host(omr_ntt_domain_t d, int encoder, uint64_t s, void* host_
   if (batch == 0) return OMR_NTT_OK;
   DeviceGuard g(d->device);
   std::lock_guard<std::mutex> lk(d->host_mu);
+  const uint64_t chunk = host_chunk(d, batch);
+  if (chunk)
+    return host_pipelined(d, static_cast<char*>(host_buf), batch, chunk,
+                          [&](void* buf, uint64_t cnt, cudaStream_t st) {
+                            return omr_ntt_encode(d, encoder, s, buf, cnt, st);
+                          });
   const size_t bytes = (size_t)d->n * batch * word_bytes(d->field);
   void* dbuf = nullptr;
   int rc = domain_scratch(d, nullptr, bytes, &dbuf, 2);

@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -403,6 +404,67 @@ int run_transform(omr_ntt_domain_s* d, int plan, bool inverse, const void* in, v
   return OMR_NTT_OK;
 }
 
+uint64_t host_chunk(const omr_ntt_domain_s* d, uint64_t batch) {
+  // chunks of >= 8 MiB, at least two of them; 0: no pipelining (one transform)
+  const uint64_t per = d->n * word_bytes(d->field);
+  uint64_t chunk = ((8ull << 20) + per - 1) / per;
+  if (chunk > batch / 2) chunk = batch / 2;
+  return batch >= 2 ? chunk : 0;
+}
+
+// Batches through host buffers: chunks of transforms flow through two device
+// buffers on three streams (copy in, transform, copy out), so the copies of
+// neighbouring chunks overlap each other and the transforms (the two copy
+// directions overlap in part on GB300's host link).  Caller holds d->host_mu.
+int host_pipelined(omr_ntt_domain_s* d, char* host, uint64_t batch, uint64_t chunk,
+                   const std::function<int(void*, uint64_t, cudaStream_t)>& op) {
+  const size_t per = (size_t)d->n * word_bytes(d->field);
+  for (auto& s : d->host_streams)
+    if (!s && cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(OMR_NTT_ERR_CUDA, "host-pipeline stream");
+  cudaStream_t sh = d->host_streams[0], sc = d->host_streams[1], sd = d->host_streams[2];
+  void* buf[2] = {nullptr, nullptr};
+  int rc = domain_scratch(d, sh, chunk * per, &buf[0], 2);
+  if (!rc) rc = domain_scratch(d, sd, chunk * per, &buf[1], 2);
+  if (rc) return rc;
+  cudaEvent_t ev[3][2] = {};  // copied in / transformed / copied out, per buffer
+  for (auto& row : ev)
+    for (auto& e : row)
+      if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        rc = fail(OMR_NTT_ERR_CUDA, "host-pipeline event");
+  for (uint64_t off = 0, i = 0; !rc && off < batch; off += chunk, i++) {
+    const int b = (int)(i & 1);
+    const uint64_t cnt = batch - off < chunk ? batch - off : chunk;
+    char* h = host + off * per;
+    if (i >= 2) cudaStreamWaitEvent(sh, ev[2][b], 0);  // buffer b copied out
+    if (cudaMemcpyAsync(buf[b], h, cnt * per, cudaMemcpyHostToDevice, sh) != cudaSuccess) {
+      rc = fail(OMR_NTT_ERR_CUDA, "host-to-device copy failed");
+      break;
+    }
+    cudaEventRecord(ev[0][b], sh);
+    cudaStreamWaitEvent(sc, ev[0][b], 0);
+    rc = op(buf[b], cnt, sc);
+    if (rc) break;
+    cudaEventRecord(ev[1][b], sc);
+    cudaStreamWaitEvent(sd, ev[1][b], 0);
+    if (cudaMemcpyAsync(h, buf[b], cnt * per, cudaMemcpyDeviceToHost, sd) != cudaSuccess) {
+      rc = fail(OMR_NTT_ERR_CUDA, "device-to-host copy failed");
+      break;
+    }
+    cudaEventRecord(ev[2][b], sd);
+  }
+  // every queued copy ends before the host buffer is handed back
+  for (cudaStream_t s : {sh, sc, sd}) {
+    cudaError_t se = cudaStreamSynchronize(s);
+    if (!rc && se != cudaSuccess) rc = fail(OMR_NTT_ERR_CUDA, cudaGetErrorString(se));
+  }
+  for (auto& row : ev)
+    for (auto& e : row)
+      if (e) cudaEventDestroy(e);
+  if (!rc) rc = omr_ntt_domain_check(d, sc);
+  return rc;
+}
+
 }  // namespace omr
 
 using namespace omr;
@@ -543,73 +605,18 @@ int omr_ntt_inverse(omr_ntt_domain_t d, int plan, const void* in, void* out, uin
   return run_transform(d, plan, true, in, out, batch, (cudaStream_t)stream);
 }
 
-// Batches through host buffers: chunks of transforms flow through two device
-// buffers on three streams (copy in, transform, copy out), so the copies of
-// neighbouring chunks overlap each other and the transforms (the host link is
-// full duplex).  Caller holds d->host_mu.
-static int host_pipelined(omr_ntt_domain_t d, int plan, bool inverse, char* host, uint64_t batch,
-                          uint64_t chunk) {
-  const size_t per = (size_t)d->n * word_bytes(d->field);
-  for (auto& s : d->host_streams)
-    if (!s && cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
-      return fail(OMR_NTT_ERR_CUDA, "host-pipeline stream");
-  cudaStream_t sh = d->host_streams[0], sc = d->host_streams[1], sd = d->host_streams[2];
-  void* buf[2] = {nullptr, nullptr};
-  int rc = domain_scratch(d, sh, chunk * per, &buf[0], 2);
-  if (!rc) rc = domain_scratch(d, sd, chunk * per, &buf[1], 2);
-  if (rc) return rc;
-  cudaEvent_t ev[3][2] = {};  // copied in / transformed / copied out, per buffer
-  for (auto& row : ev)
-    for (auto& e : row)
-      if (!rc && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
-        rc = fail(OMR_NTT_ERR_CUDA, "host-pipeline event");
-  for (uint64_t off = 0, i = 0; !rc && off < batch; off += chunk, i++) {
-    const int b = (int)(i & 1);
-    const uint64_t cnt = batch - off < chunk ? batch - off : chunk;
-    char* h = host + off * per;
-    if (i >= 2) cudaStreamWaitEvent(sh, ev[2][b], 0);  // buffer b copied out
-    if (cudaMemcpyAsync(buf[b], h, cnt * per, cudaMemcpyHostToDevice, sh) != cudaSuccess) {
-      rc = fail(OMR_NTT_ERR_CUDA, "host-to-device copy failed");
-      break;
-    }
-    cudaEventRecord(ev[0][b], sh);
-    cudaStreamWaitEvent(sc, ev[0][b], 0);
-    rc = run_transform(d, plan, inverse, buf[b], buf[b], cnt, sc);
-    if (rc) break;
-    cudaEventRecord(ev[1][b], sc);
-    cudaStreamWaitEvent(sd, ev[1][b], 0);
-    if (cudaMemcpyAsync(h, buf[b], cnt * per, cudaMemcpyDeviceToHost, sd) != cudaSuccess) {
-      rc = fail(OMR_NTT_ERR_CUDA, "device-to-host copy failed");
-      break;
-    }
-    cudaEventRecord(ev[2][b], sd);
-  }
-  // every queued copy ends before the host buffer is handed back
-  for (cudaStream_t s : {sh, sc, sd}) {
-    cudaError_t se = cudaStreamSynchronize(s);
-    if (!rc && se != cudaSuccess) rc = fail(OMR_NTT_ERR_CUDA, cudaGetErrorString(se));
-  }
-  for (auto& row : ev)
-    for (auto& e : row)
-      if (e) cudaEventDestroy(e);
-  if (!rc) rc = omr_ntt_domain_check(d, sc);
-  return rc;
-}
-
 static int host_roundtrip(omr_ntt_domain_t d, int plan, bool inverse, void* host_buf,
                           uint64_t batch) {
   if (!d || !host_buf) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
   if (batch == 0) return OMR_NTT_OK;
   DeviceGuard g(d->device);
   std::lock_guard<std::mutex> lk(d->host_mu);
-  {
-    // batches: chunks of >= 8 MiB, at least two of them
-    const uint64_t per = d->n * word_bytes(d->field);
-    uint64_t chunk = ((8ull << 20) + per - 1) / per;
-    if (chunk > batch / 2) chunk = batch / 2;
-    if (batch >= 2 && chunk >= 1)
-      return host_pipelined(d, plan, inverse, static_cast<char*>(host_buf), batch, chunk);
-  }
+  const uint64_t chunk = host_chunk(d, batch);
+  if (chunk)
+    return host_pipelined(d, static_cast<char*>(host_buf), batch, chunk,
+                          [&](void* buf, uint64_t cnt, cudaStream_t st) {
+                            return run_transform(d, plan, inverse, buf, buf, cnt, st);
+                          });
   const size_t bytes = (size_t)d->n * batch * word_bytes(d->field);
   void* dbuf = nullptr;
   cudaStream_t s = nullptr;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -64,6 +65,12 @@ int launch_cluster_transform(const omr_ntt_domain_s* d, const std::vector<PassDe
                              bool inverse, const void* in, void* out, uint64_t batch,
                              cudaStream_t stream);
 constexpr int kClusterVariant = 3;  // PlanShape::variant of the cluster plans
+// Host-buffer batches: chunk size in transforms (0: run unpipelined), and the
+// pipelined loop that applies `op(device_buf, transforms, stream)` to every
+// chunk between its copy in and copy out.  Caller holds d->host_mu.
+uint64_t host_chunk(const omr_ntt_domain_s* d, uint64_t batch);
+int host_pipelined(omr_ntt_domain_s* d, char* host, uint64_t batch, uint64_t chunk,
+                   const std::function<int(void*, uint64_t, cudaStream_t)>& op);
 // The planner's partial strategy (1 if the database or the learned selector has one).
 int planned_partial(int field, uint32_t log_n, int pattern, uint64_t count, int* strategy,
                     int* param);

@@ -125,3 +125,20 @@ def test_domain_tables_match_reference_definition():
     br = [int(v) for v in d.bitrev_twiddles]
     rev = lambda i: int(format(i, "09b")[::-1], 2)
     assert br == [tw[rev(i)] for i in range(n // 2)]
+
+
+def test_encode_host_batches_pipelined(oracle):
+    """encode_host on a batch of host transforms (pipelined chunks): a full
+    encoder and a partial one, each transform against the oracle."""
+    f, log_n, batch = BabyBear, 18, 6
+    n = 1 << log_n
+    d = NttDomain(f, n)
+    x = gen_input_seeded(f, n * batch, 808)
+    full = oracle.forward(f.id, x, batch=batch).reshape(batch, n)
+    y = x.copy()
+    WinterfellFourStep().ntt(y, d, batch=batch)
+    assert np.array_equal(y.reshape(batch, n), full)
+    s = 50
+    z = x.copy()
+    TransformDecomposition(s).ntt(z, d, batch=batch)
+    assert np.array_equal(z.reshape(batch, n)[:, :2 * s], full[:, :2 * s])
