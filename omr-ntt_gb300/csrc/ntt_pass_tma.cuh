@@ -317,8 +317,16 @@ OMR_D void issue_store(const CUtensorMap* map, const PassArgs<F>& a, uint64_t ti
 // NBUF = 2: one CTA per SM, the next tile lands while this one computes.
 // NBUF = 1: two CTAs per SM, each loads its next tile after storing the last;
 //           the other CTA keeps the SM busy meanwhile.
+// Resident CTAs the register budget is sized for: NBUF = 2 one, NBUF = 1 two,
+// or -- for the 16-elements-per-thread tiles of 32-bit fields -- as many
+// 64-register CTAs as make 1024 threads (four at 2048-point lines).
+template <class F, int LOGT, int NT, int NBUF>
+constexpr int tma_min_blocks() {
+  return (NBUF == 1 && F::WORD == 4 && LOGT >= 11 && NT < 512) ? 1024 / NT : 3 - NBUF;
+}
+
 template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW, int NBUF>
-__global__ void __launch_bounds__(NT, 3 - NBUF)
+__global__ void __launch_bounds__(NT, (tma_min_blocks<F, LOGT, NT, NBUF>()))
     ntt_tile_pass_tma(const __grid_constant__ CUtensorMap in_map,
                       const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
   using E = typename F::E;
