@@ -70,6 +70,18 @@ OMR_D typename F::Tw omega_tw(const PassArgs<F>& a, uint64_t e) {
   }
 }
 
+// Shared-memory words of the kernel: the tile, and for lines longer than the
+// CTA (more outputs than threads) one accumulator and one Horner multiplier
+// per output, which would not fit in registers.
+template <class F, int LOGT>
+constexpr size_t prefix_smem_bytes() {
+  constexpr size_t T = (size_t)1 << LOGT;
+  constexpr size_t tile = T * prefix_cols<F, LOGT>() * sizeof(typename F::E);
+  return T > (size_t)prefix_threads<F, LOGT>()
+             ? tile + T * (sizeof(typename F::E) + sizeof(typename F::Tw))
+             : tile;
+}
+
 template <class F, int LOGT>
 __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
     prefix_decomp_kernel(const PassArgs<F> a, uint32_t m, typename F::E* __restrict__ partial) {
@@ -78,27 +90,30 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
   constexpr int T = 1 << LOGT;
   constexpr int C = prefix_cols<F, LOGT>();
   constexpr int NT = prefix_threads<F, LOGT>();
-  constexpr int KMAX = T > NT ? T / NT : 1;  // outputs per thread when m > NT
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E* s = reinterpret_cast<E*>(smem_raw);
+  // m > NT (only when T > NT): outputs k = t + j NT, accumulators in smem
+  E* acc_s = s + (size_t)T * C;
+  Tw* zi_s = reinterpret_cast<Tw*>(acc_s + T);
 
   // thread -> KACT adjacent outputs x TPK column slices (m <= NT), or
   // outputs k = t + j NT (m > NT, one slice)
   uint32_t kact = 1;
   while (kact < m && kact < (uint32_t)NT) kact <<= 1;
   const uint32_t tpk = min((uint32_t)NT / kact, (uint32_t)C);
-  const uint32_t kper = (m + NT - 1) / NT;
+  const bool many = m > (uint32_t)NT;
   const uint32_t kbase = threadIdx.x % kact;
   const uint32_t slice = threadIdx.x / kact;
-  const bool active = slice < tpk;
+  const bool active = slice < tpk && kbase < m;
 
-  E acc[KMAX];
-  Tw zi[KMAX];
-#pragma unroll
-  for (int j = 0; j < KMAX; j++) {
-    acc[j] = 0;
-    const uint32_t k = kbase + j * NT;
-    zi[j] = omega_tw<F>(a, (uint64_t)0 - (uint64_t)tpk * k);  // omega_N^(-TPK k)
+  E acc = 0;
+  const Tw zi = omega_tw<F>(a, (uint64_t)0 - (uint64_t)tpk * kbase);  // omega_N^(-TPK k)
+  if constexpr (T > NT) {
+    if (many)
+      for (uint32_t k = threadIdx.x; k < m; k += NT) {  // this thread's outputs only
+        acc_s[k] = 0;
+        zi_s[k] = omega_tw<F>(a, (uint64_t)0 - (uint64_t)k);
+      }
   }
 
   const uint32_t groups = (a.L_lo + C - 1) / C;
@@ -108,44 +123,48 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
     const uint32_t llo0 = g * C;
     const int nvalid = (int)min((uint32_t)C, a.L_lo - llo0);
     prefix_rounds<F, LOGT, C, NT, 0>(a, s, a.in + llo0, nvalid);
-    if (active) {
+    if constexpr (T > NT) {
+      if (many) {
+        for (uint32_t k = threadIdx.x; k < m; k += NT) {
+          E h = acc_s[k];
+          const Tw z = zi_s[k];
 #pragma unroll
-      for (int j = 0; j < KMAX; j++) {
-        const uint32_t k = kbase + j * NT;
-        if (j < (int)kper && k < m) {
-          E h = acc[j];
-#pragma unroll 4
-          for (uint32_t c = slice; c < (uint32_t)C; c += tpk)
-            h = F::add(F::mul_tw(h, zi[j]), s[tile_idx<F, C>((int)k, (int)c)]);
-          acc[j] = h;
+          for (int c = 0; c < C; c++) h = F::add(F::mul_tw(h, z), s[tile_idx<F, C>((int)k, c)]);
+          acc_s[k] = h;
         }
       }
     }
+    if (!many && active) {
+#pragma unroll 4
+      for (uint32_t c = slice; c < (uint32_t)C; c += tpk)
+        acc = F::add(F::mul_tw(acc, zi), s[tile_idx<F, C>((int)kbase, (int)c)]);
+    }
     __syncthreads();  // the next group's first round overwrites the tile
   }
-  if (g1 > g0) {
-    const uint64_t r_last = (uint64_t)(g1 - 1) * C + (C - tpk) + slice;
-#pragma unroll
-    for (int j = 0; j < KMAX; j++) {
-      const uint32_t k = kbase + j * NT;
-      if (active && j < (int)kper && k < m) acc[j] = mul_m<F>(acc[j], omega_m<F>(a, r_last * k));
+  if constexpr (T > NT) {
+    if (many) {
+      const uint64_t r_last = (uint64_t)(g1 - 1) * C + (C - 1);
+      for (uint32_t k = threadIdx.x; k < m; k += NT)
+        partial[(uint64_t)blockIdx.x * m + k] =
+            g1 > g0 ? mul_m<F>(acc_s[k], omega_m<F>(a, r_last * k)) : (E)0;
+      return;
     }
+  }
+  if (g1 > g0 && active) {
+    const uint64_t r_last = (uint64_t)(g1 - 1) * C + (C - tpk) + slice;
+    acc = mul_m<F>(acc, omega_m<F>(a, r_last * kbase));
   }
   if (tpk > 1) {
     // combine the slices of every output: s[slice * kact + k]
-    if (active) s[slice * kact + kbase] = acc[0];
+    if (slice < tpk) s[slice * kact + kbase] = active ? acc : (E)0;
     __syncthreads();
     if (threadIdx.x < m) {
       E sum = 0;
       for (uint32_t sl = 0; sl < tpk; sl++) sum = F::add(sum, s[sl * kact + threadIdx.x]);
       partial[(uint64_t)blockIdx.x * m + threadIdx.x] = sum;
     }
-  } else {
-#pragma unroll
-    for (int j = 0; j < KMAX; j++) {
-      const uint32_t k = threadIdx.x + j * NT;
-      if (j < (int)kper && k < m) partial[(uint64_t)blockIdx.x * m + k] = acc[j];
-    }
+  } else if (threadIdx.x < m) {
+    partial[(uint64_t)blockIdx.x * m + threadIdx.x] = acc;
   }
 }
 
@@ -207,7 +226,7 @@ inline int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void
   constexpr int T = 1 << LOGT;
   constexpr int C = prefix_cols<F, LOGT>();
   constexpr int NT = prefix_threads<F, LOGT>();
-  constexpr size_t smem = (size_t)T * C * sizeof(E);
+  constexpr size_t smem = prefix_smem_bytes<F, LOGT>();
   auto kern = prefix_decomp_kernel<F, LOGT>;
   static std::atomic<int> occ_cache[64];
   int dev = 0;
