@@ -171,32 +171,53 @@ struct Goldilocks {
   OMR_D static E neg(E a) { return a ? P - a : 0ull; }
   // a + b (2^32 - 1) - c (mod p), canonical; a, c < 2^64, b < 2^32, and
   // a - c + 2^64 > EPS whenever a < c (true for every caller: c < 2^32, or a = 0)
+  //
+  // w = t + b (2^32 - 1) is one 32x32 -> 64 multiply-add (mad.lo/hi with
+  // carry), and each conditional + EPS is a multiply-add of the 0 / 1 carry by
+  // 0xffffffff: that work runs on the multiply pipe and leaves the integer ALU
+  // pipe -- the bound of the Goldilocks passes -- to the carry chains.  A flag
+  // is read only by the instruction family that set it (addc after additions,
+  // subc after subtractions): a subtraction's borrow and an addition's carry
+  // are not interchangeable in the compiled code.
   OMR_D static E reduce3(uint64_t a, uint32_t b, uint64_t c) {
     uint32_t r0, r1;
-    asm("{.reg .u32 t0, t1, m;\n\t"
-        ".reg .pred ge;\n\t"
+    asm("{.reg .u32 t0, t1, x, m;\n\t"
         "sub.cc.u32 t0, %2, %5;\n\t"    // t = a - c
         "subc.cc.u32 t1, %3, %6;\n\t"
-        "subc.u32 m, 0, 0;\n\t"
+        "subc.u32 m, 0, 0;\n\t"         // borrow mask
         "sub.cc.u32 t0, t0, m;\n\t"     // borrow: - EPS
         "subc.u32 t1, t1, 0;\n\t"
-        "sub.cc.u32 %0, 0, %4;\n\t"     // u = b 2^32 - b
-        "subc.u32 %1, %4, 0;\n\t"
-        "add.cc.u32 t0, t0, %0;\n\t"    // w = t + u
-        "addc.cc.u32 t1, t1, %1;\n\t"
-        "addc.u32 m, 0, 0;\n\t"
-        "neg.s32 m, m;\n\t"
-        "add.cc.u32 t0, t0, m;\n\t"     // carry: + EPS (cannot carry again)
+        "mad.lo.cc.u32 t0, %4, 0xffffffff, t0;\n\t"   // w = t + b (2^32 - 1)
+        "madc.hi.cc.u32 t1, %4, 0xffffffff, t1;\n\t"
+        "addc.u32 m, 0, 0;\n\t"         // carry (0 / 1)
+        "mad.lo.cc.u32 t0, m, 0xffffffff, t0;\n\t"    // carry: + EPS (cannot carry again)
         "addc.u32 t1, t1, 0;\n\t"
-        "add.cc.u32 %0, t0, -1;\n\t"    // w + EPS carries  <=>  w >= p
-        "addc.cc.u32 %1, t1, 0;\n\t"
+        "add.cc.u32 x, t0, 0xffffffff;\n\t"   // w + EPS carries  <=>  w >= p
+        "addc.cc.u32 x, t1, 0;\n\t"
         "addc.u32 m, 0, 0;\n\t"
-        "setp.ne.u32 ge, m, 0;\n\t"
-        "selp.b32 %0, %0, t0, ge;\n\t"
-        "selp.b32 %1, %1, t1, ge;}"
+        "mad.lo.cc.u32 %0, m, 0xffffffff, t0;\n\t"    // w >= p: w + EPS = w - p
+        "addc.u32 %1, t1, 0;}"
         : "=&r"(r0), "=&r"(r1)
         : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"(b), "r"((uint32_t)c),
           "r"((uint32_t)(c >> 32)));
+    return pack(r0, r1);
+  }
+  // a + b (2^32 - 1) (mod p), canonical; reduce3 with c = 0
+  OMR_D static E reduce2(uint64_t a, uint32_t b) {
+    uint32_t r0, r1;
+    asm("{.reg .u32 t0, t1, x, m;\n\t"
+        "mad.lo.cc.u32 t0, %4, 0xffffffff, %2;\n\t"
+        "madc.hi.cc.u32 t1, %4, 0xffffffff, %3;\n\t"
+        "addc.u32 m, 0, 0;\n\t"
+        "mad.lo.cc.u32 t0, m, 0xffffffff, t0;\n\t"
+        "addc.u32 t1, t1, 0;\n\t"
+        "add.cc.u32 x, t0, 0xffffffff;\n\t"
+        "addc.cc.u32 x, t1, 0;\n\t"
+        "addc.u32 m, 0, 0;\n\t"
+        "mad.lo.cc.u32 %0, m, 0xffffffff, t0;\n\t"
+        "addc.u32 %1, t1, 0;}"
+        : "=&r"(r0), "=&r"(r1)
+        : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"(b));
     return pack(r0, r1);
   }
   // reduce a 128-bit value hi 2^64 + lo:  2^64 = 2^32 - 1, 2^96 = -1
@@ -227,7 +248,7 @@ struct Goldilocks {
     if constexpr (S == 0) {
       return x;
     } else if constexpr (S < 32) {
-      return reduce3(x << S, (uint32_t)(x >> (64 - S)), 0ull);
+      return reduce2(x << S, (uint32_t)(x >> (64 - S)));
     } else if constexpr (S < 64) {
       return reduce3(x << S, (uint32_t)(x >> (64 - S)), x >> (96 - S));
     } else if constexpr (S == 64) {
