@@ -243,9 +243,9 @@ static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   size_t nsplit = 0;
   for (auto& p : plans)
     if (p.variant == 0) nsplit++;
-  // 31-bit fields: variant 2 (two CTAs per SM at <= 64 registers); Goldilocks
-  // and TeddyBear (wider arithmetic): variant 1 (double-buffered)
-  const bool narrow = field == BABYBEAR || field == KOALABEAR;
+  // 32-bit fields: variant 2 (two CTAs per SM at <= 64 registers);
+  // Goldilocks: variant 1 (double-buffered)
+  const bool narrow = field != GOLDILOCKS;
   const int cand = (int)nsplit * (narrow ? 2 : 1);  // first (balanced) split
   return cand < (int)plans.size() ? cand : 0;
 }
