@@ -174,6 +174,16 @@ std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
   return out;
 }
 
+const std::vector<PlanShape>& plan_table(uint32_t log_n) {
+  static const std::vector<std::vector<PlanShape>> table = [] {
+    std::vector<std::vector<PlanShape>> t;
+    for (uint32_t l = 0; l <= 32; l++) t.push_back(enumerate_plans(l));
+    return t;
+  }();
+  static const std::vector<PlanShape> none;
+  return log_n <= 32 ? table[log_n] : none;
+}
+
 std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanShape& shape) {
   std::vector<PassDesc> ps;
   const uint64_t N = 1ull << log_n;
@@ -644,7 +654,7 @@ int omr_ntt_inverse_host(omr_ntt_domain_t d, int plan, void* host_buf, uint64_t 
 int omr_ntt_plan_count(int field, uint32_t log_n) {
   if (!valid_field(field)) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown field id");
   if ((int)log_n > two_adicity(field)) return fail(OMR_NTT_ERR_SIZE, "log2(N) > TWO_ADICITY");
-  return (int)enumerate_plans(log_n).size();
+  return (int)plan_table(log_n).size();
 }
 
 int omr_ntt_plan_describe(int field, uint32_t log_n, int plan, char* buf, size_t cap) {
@@ -652,7 +662,7 @@ int omr_ntt_plan_describe(int field, uint32_t log_n, int plan, char* buf, size_t
   if (cnt < 0) return cnt;
   if (plan < 0) plan = default_plan(field, log_n, 1);
   if (plan >= cnt) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "plan id out of range");
-  std::string n = plan_name(field, enumerate_plans(log_n)[plan]);
+  std::string n = plan_name(field, plan_table(log_n)[plan]);
   if (buf && cap) {
     std::strncpy(buf, n.c_str(), cap - 1);
     buf[cap - 1] = 0;
@@ -667,7 +677,7 @@ int omr_ntt_plan_passes(int field, uint32_t log_n, int plan, uint64_t batch, uin
   if (plan < 0) plan = default_plan(field, log_n, batch);
   if (plan >= cnt) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "plan id out of range");
   std::vector<PassDesc> ps =
-      log_n ? build_passes(log_n, batch, enumerate_plans(log_n)[plan]) : std::vector<PassDesc>{};
+      log_n ? build_passes(log_n, batch, plan_table(log_n)[plan]) : std::vector<PassDesc>{};
   for (int i = 0; i < (int)ps.size() && i < cap && rec; i++) {
     const PassDesc& p = ps[i];
     uint64_t* r = rec + 16 * i;

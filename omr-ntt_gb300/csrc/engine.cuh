@@ -54,6 +54,8 @@ struct PlanShape {
 };
 
 std::vector<PlanShape> enumerate_plans(uint32_t log_n);
+// enumerate_plans(log_n) for log_n <= 32, built once (no allocation per call)
+const std::vector<PlanShape>& plan_table(uint32_t log_n);
 std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanShape& shape);
 int default_plan(int field, uint32_t log_n, uint64_t batch);
 // The planner's full-transform plan: planner database, learned selector, else

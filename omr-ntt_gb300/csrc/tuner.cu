@@ -40,7 +40,7 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
   (void)field;
   std::vector<Cand> v;
   const uint64_t n = 1ull << log_n;
-  const int nfull = (int)enumerate_plans(log_n).size();
+  const int nfull = (int)plan_table(log_n).size();
   if (count >= n || count == 0) {
     for (int p = 0; p < nfull; p++) v.push_back({STRAT_FULL, p});
     return v;
@@ -54,7 +54,7 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
   if (pattern == OMR_NTT_PATTERN_STRIDED && (count & (count - 1)) == 0) {
     uint32_t ls = 0;
     while ((1ull << ls) < count) ls++;
-    const int nsub = (int)enumerate_plans(ls).size();
+    const int nsub = (int)plan_table(ls).size();
     for (int p = 0; p < nsub; p++) v.push_back({STRAT_FOLD, p});
   }
   for (int p = 0; p < nfull; p++) v.push_back({STRAT_GATHER, p});
@@ -75,7 +75,7 @@ constexpr int kNumClasses = 40;
 
 // plan id of full class fc (0..11) for a 2^log_n transform, or -1
 static int full_class_plan(uint32_t log_n, int fc) {
-  const auto plans = enumerate_plans(log_n);
+  const auto& plans = plan_table(log_n);
   if (log_n == 0) return fc == 0 ? 0 : -1;
   if (fc == 3) {
     for (int i = 0; i < (int)plans.size(); i++)
@@ -233,7 +233,7 @@ static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, ui
 // Built-in heuristic (measured on GB300): the two-buffer TMA pass for the
 // headline fields' balanced split, the tile pass otherwise.
 static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
-  const auto plans = enumerate_plans(log_n);
+  const auto& plans = plan_table(log_n);
   if (plans.size() <= 1 || plans[0].split.size() < 2) return 0;
   // the one-launch cluster plan wins where latency dominates: up to 2^14, or
   // batches of 8 and more (one cluster per transform)
@@ -252,7 +252,7 @@ static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
 
 int planned_full_plan(int field, uint32_t log_n, uint64_t batch) {
   Cand c;
-  const int n = (int)enumerate_plans(log_n).size();
+  const int n = (int)plan_table(log_n).size();
   if (db_lookup(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
     return c.param;
   if (mlp_choice_cached(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
