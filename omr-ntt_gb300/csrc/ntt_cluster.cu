@@ -62,10 +62,23 @@ __global__ void __launch_bounds__(kClusterThreads)
   cluster_columns<F, LOG1, W, INV, 0>(a, ta, a.in + t * a.is_b + r * W, r * W);
   cluster.sync();  // every pass-1 tile complete and visible to the cluster
 
-  for (int idx = threadIdx.x; idx < H * N2; idx += kClusterThreads) {
+  // all of a thread's remote loads are issued before its local stores: the
+  // two tiles are reached through generic pointers the compiler cannot tell
+  // apart, so a load-store loop would wait out each remote load in turn
+  constexpr int G = H * N2 / kClusterThreads;
+  static_assert(H * N2 % kClusterThreads == 0, "whole gather rounds");
+  E g[G];
+#pragma unroll
+  for (int k = 0; k < G; k++) {
+    const int idx = threadIdx.x + k * kClusterThreads;
     const int rl = idx / N2, n2 = idx % N2;  // local row, column
     const E* peer = cluster.map_shared_rank(ta, (int)(n2 / W));
-    tb[tile_idx<F, H>(n2, rl)] = peer[tile_idx<F, W>((int)(r * H) + rl, n2 % W)];
+    g[k] = peer[tile_idx<F, W>((int)(r * H) + rl, n2 % W)];
+  }
+#pragma unroll
+  for (int k = 0; k < G; k++) {
+    const int idx = threadIdx.x + k * kClusterThreads;
+    tb[tile_idx<F, H>(idx % N2, idx / N2)] = g[k];
   }
   __syncthreads();
   all_rounds<F, LOG2, H, kClusterThreads, MODE_ROW, INV, 0>(b, tb, nullptr,
