@@ -269,6 +269,20 @@ OMR_D void do_round(const PassArgs<F>& a, typename F::E* s, const typename F::E*
       }
       dft_reg<F, LOGR, INV>(v[i]);
       const int d = ((j >> LOGNS) << (LOGNS + LOGR)) | jm;
+      // four-step twiddle of output k = d + q NS: omega_N^(line k scale) =
+      // base * step^q, base = omega_N^(line d scale), step = omega_N^(line NS
+      // scale); two table lookups per group, one product per output
+      [[maybe_unused]] E tw_cur{}, tw_step{};
+      [[maybe_unused]] bool has_tw = false;
+      if constexpr (TW && DST != DST_SMEM) {
+        has_tw = (DST == DST_STAGE || a.tw_lo != nullptr) && c < nvalid;
+        if (has_tw) {
+          const uint32_t ls = (llo0 + (uint32_t)c + lm * a.tw_line_mul_m) * a.tw_scale;
+          const uint32_t eb = (ls * (uint32_t)d) & a.tw_mask, es = (ls * (uint32_t)NS) & a.tw_mask;
+          tw_cur = F::mul_tw(a.tw_lo[eb & ((1u << kTwLoBits) - 1)], a.tw_hi[eb >> kTwLoBits]);
+          tw_step = F::mul_tw(a.tw_lo[es & ((1u << kTwLoBits) - 1)], a.tw_hi[es >> kTwLoBits]);
+        }
+      }
 #pragma unroll
       for (int q = 0; q < R; q++) {
         const int k = d + q * NS;
@@ -279,10 +293,8 @@ OMR_D void do_round(const PassArgs<F>& a, typename F::E* s, const typename F::E*
           if (c < nvalid) {
             y = v[i][q];
             if constexpr (TW) {
-              const uint32_t line = llo0 + (uint32_t)c + lm * a.tw_line_mul_m;
-              const uint32_t e = (line * (uint32_t)k * a.tw_scale) & a.tw_mask;
-              const E tm = F::mul_tw(a.tw_lo[e & ((1u << kTwLoBits) - 1)], a.tw_hi[e >> kTwLoBits]);
-              y = mul_m<F>(y, tm);
+              y = mul_m<F>(y, tw_cur);
+              if (q + 1 < R) tw_cur = F::mont_mul(tw_cur, tw_step);
             }
           }
           s[tile_idx<F, C>(k, c)] = y;
@@ -290,11 +302,9 @@ OMR_D void do_round(const PassArgs<F>& a, typename F::E* s, const typename F::E*
           if (c < nvalid) {
             E y = v[i][q];
             if constexpr (TW) {
-              if (a.tw_lo != nullptr) {
-                const uint32_t line = llo0 + (uint32_t)c + lm * a.tw_line_mul_m;
-                const uint32_t e = (line * (uint32_t)k * a.tw_scale) & a.tw_mask;
-                const E tm = F::mul_tw(a.tw_lo[e & ((1u << kTwLoBits) - 1)], a.tw_hi[e >> kTwLoBits]);
-                y = mul_m<F>(y, tm);
+              if (has_tw) {
+                y = mul_m<F>(y, tw_cur);
+                if (q + 1 < R) tw_cur = F::mont_mul(tw_cur, tw_step);
               }
             }
             if (a.has_scale) y = F::mul_tw(y, a.scale);
