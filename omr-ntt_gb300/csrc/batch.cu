@@ -156,10 +156,27 @@ OMR_D void batch_row_tile(const BatchArgs& ba, const BatchReq& r, uint32_t g, ty
   const uint32_t llo0 = g * C;
   const int nvalid = (int)min((uint32_t)C, n1 - llo0);
   const E* src = reinterpret_cast<const E*>(ba.scratch + r.scr_a) + (uint64_t)llo0 * T;
-  // stage rows (t-fast, L2-coherent loads: written by other CTAs in phase 0)
-  for (int i = threadIdx.x; i < TC; i += kBatchThreads) {
-    const int t = i % T, c = i / T;
-    s[tile_idx<F, C>(t, c)] = c < nvalid ? __ldcg(src + (uint32_t)c * T + t) : (E)0;
+  // stage rows (t-fast, L2-coherent loads: written by other CTAs in phase 0),
+  // eight loads in flight per thread before their shared-memory stores (the
+  // compiler cannot tell the two pointers apart, so a load-store loop would
+  // wait out each load in turn)
+  constexpr int PER = (TC + kBatchThreads - 1) / kBatchThreads;
+  constexpr int CH = PER < 8 ? PER : 8;
+  static_assert(PER % CH == 0, "whole chunks");
+#pragma unroll 1
+  for (int k0 = 0; k0 < PER; k0 += CH) {
+    E r[CH];
+#pragma unroll
+    for (int k = 0; k < CH; k++) {
+      const int i = threadIdx.x + (k0 + k) * kBatchThreads;
+      const int t = i % T, c = i / T;
+      r[k] = (i < TC && c < nvalid) ? __ldcg(src + (uint32_t)c * T + t) : (E)0;
+    }
+#pragma unroll
+    for (int k = 0; k < CH; k++) {
+      const int i = threadIdx.x + (k0 + k) * kBatchThreads;
+      if (i < TC) s[tile_idx<F, C>(i % T, i / T)] = r[k];
+    }
   }
   __syncthreads();
   PassArgs<F> a{};
