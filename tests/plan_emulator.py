@@ -2,7 +2,9 @@
 
 Mirrors ntt_tile_pass (omr-ntt_gb300/csrc/ntt_pass.cuh) index for index:
 tile load, the Stockham rounds of RoundPlan (radix 2^4 for every field),
-the four-step twiddle on the store and the inverse
+the four-step twiddle on the store (formed per butterfly group as the
+kernels form it, base * step^q with 32-bit index arithmetic, and checked
+against the direct exponent) and the inverse
 scale, driven by the pass records that omr_ntt_plan_passes returns.  It
 checks the host-side plan logic and the kernel's index arithmetic on the CPU.
 """
@@ -49,7 +51,9 @@ def emulate_plan(field, passes, x, log_n, inverse=False, batch=1):
                         wr = {ob + c * pd["os_lo"] + t * pd["es_out"] for t in range(T) for c in range(C)
                               if llo0 + c < pd["L_lo"]}
                         assert rd == wr, "in-place pass with mismatched read/write sets"
-                    for logr, logns in round_plan(pd["logT"], maxr):
+                    rp = round_plan(pd["logT"], maxr)
+                    chain_e = {}  # (k, c) -> four-step exponent as the kernels' chain forms it
+                    for ri, (logr, logns) in enumerate(rp):
                         R, NS = 1 << logr, 1 << logns
                         wR = pow(wT, T // R, p)
                         new = [row[:] for row in tile]
@@ -64,6 +68,14 @@ def emulate_plan(field, passes, x, log_n, inverse=False, batch=1):
                             d = ((j >> logns) << (logns + logr)) | jm
                             for q in range(R):
                                 new[d + q * NS][c] = v[q]
+                            if pd["twiddle"] and ri == len(rp) - 1:
+                                # base omega^(ls d) times step omega^(ls NS), q times;
+                                # ls and the products wrap in 32 bits as in the kernels
+                                ls = ((llo0 + c + lm * pd["tw_line_mul_m"]) * pd["tw_scale"]) & 0xFFFFFFFF
+                                eb = ((ls * d) & 0xFFFFFFFF) & (N - 1)
+                                es = ((ls * NS) & 0xFFFFFFFF) & (N - 1)
+                                for q in range(R):
+                                    chain_e[(d + q * NS, c)] = (eb + q * es) % N
                         tile = new
                     for k in range(T):
                         for c in range(C):
@@ -73,7 +85,8 @@ def emulate_plan(field, passes, x, log_n, inverse=False, batch=1):
                             if pd["twiddle"]:
                                 line = llo0 + c + lm * pd["tw_line_mul_m"]
                                 e = (line * k * pd["tw_scale"]) & (N - 1)
-                                y = y * pow(wN, e, p) % p
+                                assert chain_e[(k, c)] == e, "four-step twiddle chain exponent"
+                                y = y * pow(wN, chain_e[(k, c)], p) % p
                             if inverse and last:
                                 y = y * ninv % p
                             out_vals.append((ob + c * pd["os_lo"] + k * pd["es_out"], y))
