@@ -230,8 +230,10 @@ static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, ui
   return true;
 }
 
-// Built-in heuristic (measured on GB300): the two-buffer TMA pass for the
-// headline fields' balanced split, the tile pass otherwise.
+// Built-in heuristic (measured on GB300): the one-launch cluster plan for
+// small or batched 2^13..2^16 transforms, else the TMA pass on the balanced
+// split (two CTAs per SM for the 32-bit fields, double-buffered for
+// Goldilocks), else plan 0.
 static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   const auto& plans = plan_table(log_n);
   if (plans.size() <= 1 || plans[0].split.size() < 2) return 0;
