@@ -157,7 +157,12 @@ int omr_ntt_inverse(omr_ntt_domain_t d, int plan, const void *in, void *out, uin
  * N * batch * word_bytes above 16 MiB fails with OMR_NTT_ERR_CAPACITY.  All
  * calls share that array: calls that overlap on the GPU race on it, so order
  * them (one stream, or events).  The first call on each device looks up the
- * array's device address; make it before any stream capture on that device.
+ * array's device address; under CUDA's lazy module loading that is also when
+ * the driver loads the code and reserves the 16 MiB there, and the first
+ * launch of each kernel loads it.  So make one warm-up call per device and
+ * shape before the region that must not allocate (and before any stream
+ * capture).  The plan is the planner database's entry, else the built-in
+ * rule (the learned selector allocates on its first use and is skipped).
  * The domain is created beforehand (omr_ntt_domain_create allocates its
  * tables).  No counterpart in the reference. */
 int omr_ntt_forward_noalloc(omr_ntt_domain_t d, const void *in, void *out, uint64_t batch,

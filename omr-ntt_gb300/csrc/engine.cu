@@ -171,6 +171,13 @@ std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
   // 2^13..2^16: the balanced two-pass plan as one launch on an 8-CTA cluster
   // (appended, so the other plans keep their ids)
   if (log_n >= 13 && log_n <= 16) out.push_back(PlanShape{splits[0], kClusterVariant});
+  // the slab pass on every multi-pass split, and the wide pass on those with
+  // a 256-point pass (appended: earlier ids unchanged)
+  for (auto& s : splits)
+    if (s.size() > 1) out.push_back(PlanShape{s, kSlabVariant});
+  for (auto& s : splits)
+    if (s.size() > 1 && std::find(s.begin(), s.end(), 8) != s.end())
+      out.push_back(PlanShape{s, kWideVariant});
   return out;
 }
 
@@ -293,6 +300,8 @@ static std::string plan_name(int field, const PlanShape& s) {
     n += std::to_string(1 << s.split[i]);
   }
   if (s.variant == kClusterVariant) return n + " cluster";
+  if (s.variant == kSlabVariant) return n + " slab";
+  if (s.variant == kWideVariant) return n + " wide";
   if (s.split.size() > 1) n += v == 0 ? " tile" : (v == 1 ? " tma2buf" : " tma2cta");
   return n;
 }

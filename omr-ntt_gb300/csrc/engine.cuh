@@ -59,14 +59,17 @@ const std::vector<PlanShape>& plan_table(uint32_t log_n);
 std::vector<PassDesc> build_passes(uint32_t log_n, uint64_t batch, const PlanShape& shape);
 int default_plan(int field, uint32_t log_n, uint64_t batch);
 // The planner's full-transform plan: planner database, learned selector, else
-// built-in heuristic (tuner.cu).
-int planned_full_plan(int field, uint32_t log_n, uint64_t batch);
+// built-in heuristic (tuner.cu).  use_learned = false skips the learned
+// selector, whose first evaluation allocates its device buffers.
+int planned_full_plan(int field, uint32_t log_n, uint64_t batch, bool use_learned = true);
 // One-launch transform of a two-pass plan on an 8-CTA cluster (ntt_cluster.cu):
 // 0 launched, 1 not available for this shape (run the passes), < 0 error.
 int launch_cluster_transform(const omr_ntt_domain_s* d, const std::vector<PassDesc>& ps,
                              bool inverse, const void* in, void* out, uint64_t batch,
                              cudaStream_t stream);
 constexpr int kClusterVariant = 3;  // PlanShape::variant of the cluster plans
+constexpr int kSlabVariant = 4;     // PlanShape::variant of the slab-pass plans (ntt_pass_slab.cuh)
+constexpr int kWideVariant = 5;     // 256-point passes on 128-byte-wide tiles (ntt_pass_wide.cuh)
 // Host-buffer batches: chunk size in transforms (0: run unpipelined), and the
 // pipelined loop that applies `op(device_buf, transforms, stream)` to every
 // chunk between its copy in and copy out.  Caller holds d->host_mu.

@@ -6,7 +6,9 @@
 #include <atomic>
 
 #include "engine.cuh"
+#include "ntt_pass_slab.cuh"
 #include "ntt_pass_tma.cuh"
+#include "ntt_pass_wide.cuh"
 
 namespace omr {
 
@@ -65,6 +67,7 @@ constexpr bool has_tma_pass() {
 }
 inline int effective_variant(int field, int mode, int logT, int variant) {
   if (variant <= 0 || mode == MODE_LINE || logT < 8) return 0;
+  if (variant == kSlabVariant || variant == kWideVariant) return variant;
   int v = variant > 2 ? 2 : variant;
   if (!((tma_variant_mask(field) >> (v - 1)) & 1)) v = 3 - v;
   return v;
@@ -75,7 +78,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 constexpr size_t kMaxDynSmem = 227 * 1024 - 1024;  // leaves room for the static mbarriers
 
 static inline CUresult encode_2d(CUtensorMap* map, int word, const void* base, uint64_t dim0,
-                                 uint64_t dim1, uint64_t pitch_words, uint32_t box0, uint32_t box1) {
+                                 uint64_t dim1, uint64_t pitch_words, uint32_t box0, uint32_t box1,
+                                 CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE) {
   auto enc = tensor_map_encoder();
   if (!enc) return CUDA_ERROR_NOT_SUPPORTED;
   cuuint64_t dims[2] = {dim0, dim1};
@@ -84,6 +88,20 @@ static inline CUresult encode_2d(CUtensorMap* map, int word, const void* base, u
   cuuint32_t estr[2] = {1, 1};
   return enc(map, word == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 2,
              const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
+static inline CUresult encode_4d(CUtensorMap* map, int word, const void* base, const uint64_t (&dims)[4],
+                                 const uint64_t (&stride_words)[3], const uint32_t (&box)[4]) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return CUDA_ERROR_NOT_SUPPORTED;
+  cuuint64_t d[4] = {dims[0], dims[1], dims[2], dims[3]};
+  cuuint64_t st[3] = {stride_words[0] * (cuuint64_t)word, stride_words[1] * (cuuint64_t)word,
+                      stride_words[2] * (cuuint64_t)word};
+  cuuint32_t bx[4] = {box[0], box[1], box[2], box[3]};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(map, word == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 4,
+             const_cast<void*>(base), d, st, bx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
@@ -160,6 +178,100 @@ int launch_tma_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   return launch_tma_k<F, LOGT, MODE, INV, false, NBUF>(a, err, stream);
 }
 
+// The slab pass (ntt_pass_slab.cuh) at 256..4096-point lines.  Returns 1
+// ("not taken") when the geometry does not suit it; the caller then runs
+// variant 0.  Column passes always apply the four-step twiddle, row passes
+// never do.
+template <class F, int LOGT, int MODE, bool INV>
+int launch_slab_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
+  constexpr bool TW = MODE == MODE_COL;
+  if (!tma_geometry_ok<F>(a, LOGT, MODE) || (a.tw_lo != nullptr) != TW) return 1;
+  constexpr int C = slab_cols<F>();
+  constexpr int NT = slab_threads<LOGT>();
+  constexpr uint64_t T = 1ull << LOGT, R0 = T / 256;
+  constexpr size_t smem = slab_smem_bytes<F, LOGT>();
+  static_assert(smem <= kMaxDynSmem, "slab pass tile does not fit in shared memory");
+  auto kern = ntt_slab_pass<F, LOGT, MODE, INV, TW>;
+  static std::atomic<int> occ_cache[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int occ = occ_cache[dev & 63].load();
+  if (occ == 0) {
+    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, NT, smem));
+    if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "slab pass does not fit on an SM");
+    occ_cache[dev & 63] = occ;
+  }
+  const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
+  if (ntiles == 0) return OMR_NTT_OK;
+  CUtensorMap in_map, out_map;
+  memset(&in_map, 0, sizeof(in_map));
+  CUresult r = CUDA_SUCCESS;
+  const uint32_t box[4] = {(uint32_t)C, 256u, 1u, 1u};  // one slab per store
+  if constexpr (MODE == MODE_COL) {
+    const uint64_t L = a.L_lo, outer = (uint64_t)a.L_m * a.L_b;
+    r = encode_2d(&in_map, F::WORD, a.in, L, T * outer, L, C, 256);
+    if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (slab load) failed");
+    const uint64_t dims[4] = {L, 256, R0, outer};
+    const uint64_t strides[3] = {R0 * L, L, T * L};  // output row kk = k1 + R0 (a + 16 b)
+    r = encode_4d(&out_map, F::WORD, a.out, dims, strides, box);
+  } else {
+    const uint64_t w = (uint64_t)a.L_lo * a.L_m;
+    const uint64_t dims[4] = {w, 256, R0, a.L_b};
+    const uint64_t strides[3] = {R0 * w, w, T * w};
+    r = encode_4d(&out_map, F::WORD, a.out, dims, strides, box);
+  }
+  if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (slab store) failed");
+  const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
+  const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
+  kern<<<grid, NT, smem, stream>>>(in_map, out_map, a, err);
+  OMR_CUDA_TRY(cudaGetLastError());
+  return OMR_NTT_OK;
+}
+
+// The wide pass (ntt_pass_wide.cuh) at 256-point lines, 128 bytes of lines
+// per tile.  Returns 1 ("not taken") when the geometry does not suit it.
+template <class F, int MODE, bool INV>
+int launch_wide_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
+  constexpr bool TW = MODE == MODE_COL;
+  constexpr int C = wide_cols<F>();
+  if (a.L_lo % C || !tma_geometry_ok<F>(a, 8, MODE) || (a.tw_lo != nullptr) != TW) return 1;
+  constexpr size_t smem = wide_smem_bytes<F>();
+  static_assert(smem <= kMaxDynSmem, "wide pass does not fit in shared memory");
+  auto kern = ntt_wide_pass<F, MODE, INV, TW>;
+  static std::atomic<int> occ_cache[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int occ = occ_cache[dev & 63].load();
+  if (occ == 0) {
+    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWideThreads, smem));
+    if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "wide pass does not fit on an SM");
+    occ_cache[dev & 63] = occ;
+  }
+  const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
+  if (ntiles == 0) return OMR_NTT_OK;
+  CUtensorMap in_map, out_map;
+  memset(&in_map, 0, sizeof(in_map));
+  CUresult r;
+  const CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_128B;
+  if constexpr (MODE == MODE_COL) {
+    const uint64_t rows = 256ull * a.L_m * a.L_b;
+    r = encode_2d(&in_map, F::WORD, a.in, a.L_lo, rows, a.L_lo, C, 256, sw);
+    if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (wide load) failed");
+    r = encode_2d(&out_map, F::WORD, a.out, a.L_lo, rows, a.L_lo, C, 256, sw);
+  } else {
+    const uint64_t w = (uint64_t)a.L_lo * a.L_m;
+    r = encode_2d(&out_map, F::WORD, a.out, w, 256ull * a.L_b, w, C, 256, sw);
+  }
+  if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (wide store) failed");
+  const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
+  const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
+  kern<<<grid, kWideThreads, smem, stream>>>(in_map, out_map, a, err);
+  OMR_CUDA_TRY(cudaGetLastError());
+  return OMR_NTT_OK;
+}
+
 // Defined here, instantiated once per (field, mode, direction) in
 // pass_<field>_<mode>_<dir>.cu; the extern declarations below stop every
 // other translation unit from instantiating the kernels again.
@@ -175,7 +287,25 @@ template <class F, int MODE, bool INV>
 int launch_pass_dir(int logT, int variant, const PassArgs<F>& a, uint64_t blocks, int* err,
                     cudaStream_t s) {
   if constexpr (MODE != MODE_LINE && has_tma_pass<F>()) {
-    if (variant >= 1) {
+    if (variant == kWideVariant) {
+      // 256-point passes on the wide tiles; other line lengths of the plan
+      // take the slab pass
+      int rc = logT == 8 ? launch_wide_t<F, MODE, INV>(a, err, s) : 1;
+      if (rc != 1) return rc;
+      variant = kSlabVariant;
+    }
+    if (variant == kSlabVariant) {
+      int rc = 1;
+      switch (logT) {
+        case 8: rc = launch_slab_t<F, 8, MODE, INV>(a, err, s); break;
+        case 9: rc = launch_slab_t<F, 9, MODE, INV>(a, err, s); break;
+        case 10: rc = launch_slab_t<F, 10, MODE, INV>(a, err, s); break;
+        case 11: rc = launch_slab_t<F, 11, MODE, INV>(a, err, s); break;
+        case 12: rc = launch_slab_t<F, 12, MODE, INV>(a, err, s); break;
+        default: break;
+      }
+      if (rc != 1) return rc;
+    } else if (variant >= 1) {
       int rc = 1;
       switch (logT * 4 + variant) {
         case 8 * 4 + 1: rc = launch_tma_compiled<F, 8, MODE, INV, 2>(a, err, s); break;

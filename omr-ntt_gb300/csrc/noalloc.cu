@@ -19,8 +19,15 @@
 //   * the array keeps the previous call's contents; the first pass overwrites
 //     every word the later passes read, so nothing needs clearing;
 //   * the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress, with that device current); make that first call
-//     before any stream capture on the device.
+//     (cudaGetSymbolAddress, with that device current).  With CUDA's lazy
+//     module loading that lookup is also when the driver loads this code and
+//     reserves the 16 MiB on the device, and the first launch of each kernel
+//     loads that kernel: make one warm-up call per device and shape before
+//     the region that must not allocate (and before any stream capture);
+//   * the plan is the planner database's entry for the shape, else the
+//     built-in rule; the learned selector is not consulted, because its first
+//     evaluation allocates the network's device buffers.  Plans are
+//     tabulated once per log N, so choosing one allocates nothing.
 // The domain itself (its twiddle tables) is created beforehand with
 // omr_ntt_domain_create, outside the allocation-free region.
 #include <cuda_runtime.h>
@@ -64,19 +71,26 @@ extern "C" int omr_ntt_forward_noalloc(omr_ntt_domain_t d, const void* in, void*
                                        uint64_t batch, void* stream) {
   if (!d || !in || !out) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "null argument");
   if (batch == 0) return OMR_NTT_OK;
-  const size_t bytes = (size_t)d->n * batch * word_bytes(d->field);
-  if (d->n * batch > ((uint64_t)1 << 40) || bytes > kNoAllocScratchBytes)
+  // capacity by division first: N * batch * word could wrap for a huge batch
+  const uint64_t per = d->n * (uint64_t)word_bytes(d->field);
+  if (batch > kNoAllocScratchBytes / per)
     return fail(OMR_NTT_ERR_CAPACITY,
-                "omr_ntt_forward_noalloc: N * batch * word = " + std::to_string(bytes) +
-                    " bytes exceeds the 16 MiB static scratch; use omr_ntt_forward");
+                "omr_ntt_forward_noalloc: N * batch * word = " + std::to_string(per) + " * " +
+                    std::to_string(batch) + " bytes exceeds the 16 MiB static scratch; use omr_ntt_forward");
+  const size_t bytes = (size_t)(per * batch);
   DeviceGuard g(d->device);
   cudaStream_t st = (cudaStream_t)stream;
   if (d->log_n == 0) {
     if (in != out) OMR_CUDA_TRY(cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, st));
     return OMR_NTT_OK;
   }
-  const int plan = default_plan(d->field, d->log_n, batch);
+  const int plan = planned_full_plan(d->field, d->log_n, batch, /*use_learned=*/false);
   const std::vector<PassDesc> ps = build_passes(d->log_n, batch, d->plans[plan]);
+  if (d->plans[plan].variant == kClusterVariant) {
+    // the one-launch cluster plan keeps its intermediate in shared memory
+    int rc = launch_cluster_transform(d, ps, false, in, out, batch, st);
+    if (rc <= 0) return rc;  // launched, or an error; 1: run the passes below
+  }
   void* scratch = nullptr;
   if (ps.size() > 1) {
     int rc = noalloc_scratch_address(d->device, &scratch);

@@ -1,0 +1,303 @@
+// ntt_pass_wide.cuh -- persistent, double-buffered pass of 256-point lines on
+// 128-byte-wide tiles.
+//
+// How fast a four-step pass can move its data depends on the width of its
+// tile rows: on GB300 a copy in the pattern of a column pass (rows 16 KB
+// apart) moves 2 x 64 MB in 43 us with 16-byte rows, 32 us with 32-byte rows,
+// 27 us with 64-byte rows and 23 us -- the speed of a contiguous copy -- with
+// 128-byte rows.  A 4096-point line fills 64 KB of shared memory with only 16
+// bytes of lines per row; a 256-point line allows 128 bytes of lines per row
+// in 32 KB.  So this pass takes C = 128 / word lines (32 for the 32-bit
+// fields, 16 for Goldilocks) of 256 points per tile:
+//
+//   * column passes: one 2-D TMA box [C lines x 256 rows] per tile, landed
+//     with the 128-byte swizzle (16-byte chunk ch of row r at chunk
+//     ch ^ (r mod 8)), so every lane access below is conflict-free;
+//     row passes: one 1-D bulk copy per line into a padded line-major layout;
+//   * warp w owns the 16-byte column group w (4 or 2 lines); its lanes run
+//     the 256-point transforms of those lines as 16 x 16 (radix-16 round,
+//     twiddle omega_256^(l a), exchange through the warp's own column group
+//     with an XOR swizzle and __syncwarp, radix-16 round), then the four-step
+//     twiddle (column passes) and the inverse scale;
+//   * the results go back as 128-byte rows k = a + 16 b (natural order; a
+//     256-point line needs no output permutation) and one 2-D TMA store
+//     writes the tile;
+//   * two tile buffers: the next tile lands while this one computes.
+// Per tile that is one CTA barrier for column passes (every warp's results
+// in the buffer before the store) and two for row passes (the lines are
+// re-laid as rows in place).  Waits are bounded as in the other passes.
+//
+// The 256-point line transform is the same 16 x 16 split as the slab pass
+// (ntt_pass_slab.cuh), i.e. the reference's four-step decomposition
+// (src/encoders/winterfell_four_step.rs:31-81) within a line.
+#pragma once
+#include <cuda.h>
+
+#include "ntt_pass_slab.cuh"
+
+namespace omr {
+
+template <class F>
+constexpr int wide_cols() {
+  return 128 / F::WORD;  // lines per tile
+}
+constexpr int kWideThreads = 256;  // 8 warps: one per 16-byte column group
+template <class F>
+constexpr int wide_line_bytes() {
+  return 256 * F::WORD + 32;  // row-pass line-major layout (padded)
+}
+template <class F>
+constexpr int wide_buf_bytes() {  // a 1024-byte multiple (128-byte swizzle atoms)
+  constexpr int a = 256 * 128, b = wide_cols<F>() * wide_line_bytes<F>();
+  return ((a > b ? a : b) + 1023) / 1024 * 1024;
+}
+template <class F>
+constexpr size_t wide_smem_bytes() {
+  return 2 * (size_t)wide_buf_bytes<F>() + 15 * 16 * sizeof(typename F::Tw) + 1024;
+}
+
+// 128-byte-swizzled row layout: byte of (row r, 16-byte chunk ch, offset o)
+OMR_D int wide_sw(int r, int ch, int o) { return r * 128 + ((ch ^ (r & 7)) << 4) + o; }
+
+// The column unit u (8 bytes) of column group w, row r.
+template <class F, bool ROWS_LAYOUT>
+OMR_D void wide_load_unit(const unsigned char* s, int r, int w, int u, typename F::E* dst) {
+  constexpr int VPU = slab_vpu<F>();
+  if constexpr (ROWS_LAYOUT) {
+    const unsigned char* p = s + wide_sw(r, w, u * 8);
+    if constexpr (F::WORD == 4) {
+      const uint2 x = *reinterpret_cast<const uint2*>(p);
+      dst[0] = x.x;
+      dst[1] = x.y;
+    } else {
+      dst[0] = *reinterpret_cast<const uint64_t*>(p);
+    }
+  } else {  // line-major: line (w * 16 + u * 8) / word + c
+#pragma unroll
+    for (int c = 0; c < VPU; c++)
+      dst[c] = *reinterpret_cast<const typename F::E*>(
+          s + (w * (16 / F::WORD) + u * VPU + c) * wide_line_bytes<F>() + r * F::WORD);
+  }
+}
+template <class F, bool ROWS_LAYOUT>
+OMR_D void wide_store_unit(unsigned char* s, int r, int w, int u, const typename F::E* src) {
+  constexpr int VPU = slab_vpu<F>();
+  if constexpr (ROWS_LAYOUT) {
+    unsigned char* p = s + wide_sw(r, w, u * 8);
+    if constexpr (F::WORD == 4)
+      *reinterpret_cast<uint2*>(p) = make_uint2(src[0], src[1]);
+    else
+      *reinterpret_cast<uint64_t*>(p) = src[0];
+  } else {
+#pragma unroll
+    for (int c = 0; c < VPU; c++)
+      *reinterpret_cast<typename F::E*>(s + (w * (16 / F::WORD) + u * VPU + c) * wide_line_bytes<F>() +
+                                        r * F::WORD) = src[c];
+  }
+}
+
+template <class F, int MODE>
+OMR_D void wide_issue_load(const CUtensorMap* map, const PassArgs<F>& a, uint64_t tile,
+                           unsigned char* buf, uint64_t* bar) {
+  using E = typename F::E;
+  constexpr int C = wide_cols<F>();
+  uint32_t g, lm;
+  uint64_t lb;
+  tile_coords<F, C>(a, tile, g, lm, lb);
+  mbar_arrive_expect_tx(bar, (uint32_t)(256 * C * F::WORD));
+  if constexpr (MODE == MODE_COL) {
+    tma_load_2d(buf, map, (int)(g * C), (int)((lb * a.L_m + lm) * 256ull), bar);
+  } else {
+    const E* src = a.in + (lb * a.is_b + lm * a.is_m + (uint64_t)(g * C) * a.is_lo);
+#pragma unroll 1
+    for (int c = 0; c < C; c++)
+      bulk_load(buf + c * wide_line_bytes<F>(), src + (uint64_t)c * a.is_lo, 256 * F::WORD, bar);
+  }
+}
+
+template <class F, int MODE>
+OMR_D void wide_issue_store(const CUtensorMap* map, const PassArgs<F>& a, uint64_t tile,
+                            const unsigned char* buf) {
+  constexpr int C = wide_cols<F>();
+  uint32_t g, lm;
+  uint64_t lb;
+  tile_coords<F, C>(a, tile, g, lm, lb);
+  if constexpr (MODE == MODE_COL)
+    tma_store_2d(map, (int)(g * C), (int)((lb * a.L_m + lm) * 256ull), buf);
+  else
+    tma_store_2d(map, (int)(g * C + lm * (uint32_t)a.os_m), (int)(lb * 256ull), buf);
+  bulk_commit();
+}
+
+// One warp: the 256-point transforms of column group w.  The results are
+// left in registers, v[c][b] = line entry a + 16 b (a = lane & 15); column
+// passes also write them to the swizzled rows in place, row passes re-lay
+// them as rows after a CTA barrier (their lines span every column group).
+template <class F, int MODE, bool INV, bool TW>
+OMR_D void wide_lines(const PassArgs<F>& a, unsigned char* s, const typename F::Tw* tab1, int w,
+                      uint32_t llo0, uint32_t lm, typename F::E (&v)[slab_vpu<F>()][16]) {
+  using E = typename F::E;
+  constexpr int VPU = slab_vpu<F>();
+  constexpr bool ROWS = MODE == MODE_COL;
+  const int lane = threadIdx.x & 31;
+  const int l = lane & 15, u = lane >> 4;
+#pragma unroll
+  for (int m = 0; m < 16; m++) {
+    E x[VPU];
+    wide_load_unit<F, ROWS>(s, l + 16 * m, w, u, x);
+#pragma unroll
+    for (int c = 0; c < VPU; c++) v[c][m] = x[c];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < VPU; c++) dft_reg<F, 4, INV>(v[c]);
+#pragma unroll
+  for (int aa = 1; aa < 16; aa++) {
+    const typename F::Tw t = tab1[(aa - 1) * 16 + l];
+#pragma unroll
+    for (int c = 0; c < VPU; c++) v[c][aa] = F::mul_tw(v[c][aa], t);
+  }
+#pragma unroll
+  for (int aa = 0; aa < 16; aa++) {
+    E x[VPU];
+#pragma unroll
+    for (int c = 0; c < VPU; c++) x[c] = v[c][aa];
+    wide_store_unit<F, ROWS>(s, 16 * aa + (l ^ aa), w, u, x);
+  }
+  __syncwarp();
+  const int am = l;
+#pragma unroll
+  for (int ll = 0; ll < 16; ll++) {
+    E x[VPU];
+    wide_load_unit<F, ROWS>(s, 16 * am + (ll ^ am), w, u, x);
+#pragma unroll
+    for (int c = 0; c < VPU; c++) v[c][ll] = x[c];
+  }
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < VPU; c++) dft_reg<F, 4, INV>(v[c]);
+  // outputs b = 0..15 are line entries am + 16 b
+  if constexpr (TW) {
+#pragma unroll
+    for (int c = 0; c < VPU; c++) {
+      const uint32_t line = llo0 + (uint32_t)(w * (16 / F::WORD) + u * VPU + c) + lm * a.tw_line_mul_m;
+      const uint32_t ls = line * a.tw_scale;
+      const uint32_t e0 = (ls * (uint32_t)am) & a.tw_mask;
+      const uint32_t es = (ls * 16u) & a.tw_mask;
+      E t = F::mul_tw(__ldg(&a.tw_lo[e0 & ((1u << kTwLoBits) - 1)]), a.tw_hi[e0 >> kTwLoBits]);
+      const E step = F::mul_tw(__ldg(&a.tw_lo[es & ((1u << kTwLoBits) - 1)]), a.tw_hi[es >> kTwLoBits]);
+#pragma unroll
+      for (int b = 0; b < 16; b++) {
+        v[c][b] = mul_m<F>(v[c][b], t);
+        if (b + 1 < 16) t = F::mont_mul(t, step);
+      }
+    }
+  }
+  if (a.has_scale) {
+#pragma unroll
+    for (int c = 0; c < VPU; c++)
+#pragma unroll
+      for (int b = 0; b < 16; b++) v[c][b] = F::mul_tw(v[c][b], a.scale);
+  }
+  if constexpr (ROWS) {
+#pragma unroll
+    for (int b = 0; b < 16; b++) {
+      E x[VPU];
+#pragma unroll
+      for (int c = 0; c < VPU; c++) x[c] = v[c][b];
+      wide_store_unit<F, true>(s, am + 16 * b, w, u, x);
+    }
+  }
+}
+
+template <class F, int MODE, bool INV, bool TW>
+__global__ void __launch_bounds__(kWideThreads, 3)  // shared memory holds three CTAs an SM
+    ntt_wide_pass(const __grid_constant__ CUtensorMap in_map,
+                  const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int C = wide_cols<F>(), VPU = slab_vpu<F>();
+  constexpr int BB = wide_buf_bytes<F>();
+  extern __shared__ __align__(1024) unsigned char wide_smem_raw[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ int abort_flag;
+  unsigned char* base = wide_smem_raw + ((1024u - (smem_u32(wide_smem_raw) & 1023u)) & 1023u);
+  Tw* tab1 = reinterpret_cast<Tw*>(base + 2 * BB);
+  const int warp = threadIdx.x >> 5;
+
+  const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
+  uint64_t tile = blockIdx.x;
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_mbar_init();
+    fence_proxy_async();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  uint32_t outstanding = 0;  // bit b: a load into buffer b has not been waited for
+  if (threadIdx.x == 0) {
+    if (tile < ntiles) {
+      wide_issue_load<F, MODE>(&in_map, a, tile, base, &bars[0]);
+      outstanding |= 1u;
+    }
+    if (tile + gridDim.x < ntiles) {
+      wide_issue_load<F, MODE>(&in_map, a, tile + gridDim.x, base + BB, &bars[1]);
+      outstanding |= 2u;
+    }
+  }
+  for (int i = threadIdx.x; i < 15 * 16; i += kWideThreads) {
+    const int aa = i / 16 + 1, l = i % 16;
+    tab1[i] = a.roots[(uint32_t)(l * aa) * a.roots_stride];  // omega_256^(l a)
+  }
+  __syncthreads();
+
+  uint32_t phase = 0;
+  for (int it = 0; tile < ntiles; tile += gridDim.x, it++) {
+    const int b = it & 1;
+    unsigned char* s = base + b * BB;
+    if (mbar_wait_bounded(&bars[b], (phase >> b) & 1)) {
+      phase ^= 1u << b;
+      outstanding &= ~(1u << b);
+    } else {
+      atomicExch(err, OMR_NTT_ERR_TIMEOUT);
+      abort_flag = 1;
+    }
+    uint32_t g, lm;
+    uint64_t lb;
+    tile_coords<F, C>(a, tile, g, lm, lb);
+    E v[VPU][16];
+    wide_lines<F, MODE, INV, TW>(a, s, tab1, warp, g * C, lm, v);
+    if constexpr (MODE != MODE_COL) {
+      // every warp has read its lines: re-lay the results as swizzled rows
+      __syncthreads();
+      const int lane = threadIdx.x & 31;
+#pragma unroll
+      for (int bb = 0; bb < 16; bb++) {
+        E x[VPU];
+#pragma unroll
+        for (int c = 0; c < VPU; c++) x[c] = v[c][bb];
+        wide_store_unit<F, true>(s, (lane & 15) + 16 * bb, warp, lane >> 4, x);
+      }
+    }
+    fence_proxy_async();  // this thread's writes become visible to the TMA store
+    __syncthreads();
+    if (abort_flag) break;
+    if (threadIdx.x == 0) {
+      wide_issue_store<F, MODE>(&out_map, a, tile, s);
+      if (tile + 2ull * gridDim.x < ntiles) {
+        bulk_wait_read_all();  // the store has read the buffer
+        fence_proxy_async();
+        wide_issue_load<F, MODE>(&in_map, a, tile + 2ull * gridDim.x, s, &bars[b]);
+        outstanding |= 1u << b;
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    bulk_wait_all();
+    for (int bb = 0; bb < 2; bb++)
+      if ((outstanding >> bb) & 1) mbar_wait_bounded(&bars[bb], (phase >> bb) & 1);
+  }
+}
+
+}  // namespace omr

@@ -252,12 +252,13 @@ static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   return cand < (int)plans.size() ? cand : 0;
 }
 
-int planned_full_plan(int field, uint32_t log_n, uint64_t batch) {
+int planned_full_plan(int field, uint32_t log_n, uint64_t batch, bool use_learned) {
   Cand c;
   const int n = (int)plan_table(log_n).size();
   if (db_lookup(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
     return c.param;
-  if (mlp_choice_cached(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL && c.param < n)
+  if (use_learned && mlp_choice_cached(field, log_n, batch, -1, 0, &c) && c.strategy == STRAT_FULL &&
+      c.param < n)
     return c.param;
   return heuristic_full_plan(field, log_n, batch);
 }

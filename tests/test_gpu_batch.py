@@ -11,25 +11,24 @@ from omr_ntt.fields import BabyBear, Goldilocks
 pytestmark = pytest.mark.gpu
 
 
-def _device_inputs(nbytes, seed):
-    """Canonical words for both fields: 32-bit lanes below 2^30."""
-    import torch
+def _canonical_arena(reqs, nbytes, seed):
+    """Host input arena with seeded words uniform over the whole of [0, p) of
+    each request's field (numpy's bounded integer generator)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    arena = np.zeros(nbytes, dtype=np.uint8)
+    for r in reqs:
+        x = rng.integers(0, r.field.p, size=r.n, dtype=r.field.dtype)
+        arena[r.in_off:r.in_off + x.nbytes] = x.view(np.uint8)
+    return arena
 
-    g = torch.Generator(device="cuda").manual_seed(seed)
-    lanes = torch.randint(0, 1 << 30, ((nbytes + 3) // 4,), dtype=torch.int32, device="cuda", generator=g)
-    return lanes.view(torch.uint8)[:nbytes]
 
-
-def _run(reqs, seed, per_request=False, device_inputs=False):
+def _run(reqs, seed, per_request=False, host_in=None):
     import torch
 
     ib, ob = layout(reqs)
-    if device_inputs:
-        host_in = None
-        d_in = _device_inputs(ib, seed)
-    else:
+    if host_in is None:
         host_in = fill_inputs(reqs, ib, seed)
-        d_in = torch.from_numpy(host_in).cuda()
+    d_in = torch.from_numpy(host_in).cuda()
     d_out = torch.zeros(max(ob, 1), dtype=torch.uint8, device="cuda")
     b = Batch(reqs)
     if per_request:
@@ -74,13 +73,40 @@ def test_graph_replay_and_rerun(oracle):
         assert np.array_equal(out[r.out_off:r.out_off + 16].view(np.uint32), exp)
 
 
-def test_full_mixed_workload_matches_per_request():
+def _check_against_oracle(oracle, reqs, host_in, out, which):
+    for i in which:
+        r = reqs[i]
+        w = r.field.word_bytes
+        x = host_in[r.in_off:r.in_off + r.n * w].view(r.field.dtype)
+        assert int(x.max()) < r.field.p
+        full = oracle.inverse(r.field.id, x) if r.inverse else oracle.forward(r.field.id, x)
+        exp = full if r.indices is None else full[r.indices.astype(np.int64)]
+        got = out[r.out_off:r.out_off + r.out_words * w].view(r.field.dtype)
+        assert np.array_equal(got, exp), (i, r.field.name, r.log_n, r.inverse, r.indices is not None)
+
+
+def test_full_mixed_workload_matches_per_request(oracle):
+    """The 4096-request workload (inputs uniform over [0, p) of each field):
+    the persistent batch equals the per-request kernels word for word, and a
+    seeded sample of 64 requests with log n in [16, 20] -- both fields,
+    forward and inverse, full and index-set outputs -- equals the oracle."""
     reqs = mixed_requests(2024, count=4096)
-    _, out_batch, b = _run(reqs, 5, device_inputs=True)
+    ib, _ = layout(reqs)
+    host_in, out_batch, b = _run(reqs, 5, host_in=_canonical_arena(reqs, ib, 5))
     info = b.info()
     assert info["requests"] == 4096 and info["tasks"] > 4096
     del b
-    _, out_plain, _ = _run(reqs, 5, per_request=True, device_inputs=True)
+    # eight requests of each field x direction x output-set kind, log n >= 16
+    rng = np.random.Generator(np.random.PCG64(99))
+    kinds = {}
+    for i, r in enumerate(reqs):
+        if r.log_n >= 16:
+            kinds.setdefault((r.field.name, r.inverse, r.indices is not None), []).append(i)
+    assert len(kinds) == 8, sorted(kinds)
+    sample = sorted(j for v in kinds.values() for j in rng.choice(v, size=8, replace=False).tolist())
+    assert {reqs[i].log_n for i in sample} == {16, 17, 18, 19, 20}
+    _check_against_oracle(oracle, reqs, host_in, out_batch, sample)
+    _, out_plain, _ = _run(reqs, 5, per_request=True, host_in=host_in)
     assert np.array_equal(out_batch, out_plain)
 
 

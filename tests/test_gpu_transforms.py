@@ -107,9 +107,10 @@ def test_batch_64_of_2_20(oracle, field):
     yd = xd.clone()
     omr_ntt.forward(d, yd, batch=batch)
     y = to_host(yd, field.dtype)
-    for b in (0, 1, 37, 63):
+    exp = oracle.forward(field.id, x, batch=batch)
+    for b in range(batch):  # every segment of the batch
         seg = slice(b * n, (b + 1) * n)
-        assert np.array_equal(y[seg], oracle.forward(field.id, x[seg])), b
+        assert np.array_equal(y[seg], exp[seg]), b
     omr_ntt.inverse(d, yd, batch=batch)
     assert np.array_equal(to_host(yd, field.dtype), x)
 
