@@ -134,12 +134,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def workload_config(field, log_n):
+    """The `config` both arms print (the same workload, so the same dict)."""
+    return {"workload": f"{field.name} forward NTT n=2^{log_n}, batch 1",
+            "field": field.name, "log_n": log_n, "batch": 1}
+
+
 def cpu_baseline(field, log_n, seconds, steps=None):
     """The oracle's WinterfellFourStep (the reference's parallel four-step,
-    restated in C with OpenMP) on all host cores; bounded sample."""
+    restated in C with OpenMP) on all host cores, built for the host CPU
+    family; bounded sample.  Returns (Gelem/s, cores, samples, times, flags)."""
     import numpy as np
     from oracle import oracle
 
+    flags = oracle.use_tuned_build()
     oracle.set_threads(0)
     cores = oracle.get_threads()
     n = 1 << log_n
@@ -151,7 +159,7 @@ def cpu_baseline(field, log_n, seconds, steps=None):
         t0 = time.perf_counter()
         oracle.ntt(field.id, x, "WinterfellFourStep")
         times.append(time.perf_counter() - t0)
-    return n * len(times) / sum(times) / 1e9, cores, len(times), times
+    return n * len(times) / sum(times) / 1e9, cores, len(times), times, flags
 
 
 def cpu_config_samples(extras, partial, headline_ms, field, log_n):
@@ -204,17 +212,16 @@ def run_reference(args):
     field = field_by_name(args.field)
     n = 1 << args.log_n
     cpu_baseline(field, args.log_n, 0, steps=max(1, args.warmup))
-    val, cores, cnt, times = cpu_baseline(field, args.log_n, 0, steps=args.steps)
+    val, cores, cnt, times, flags = cpu_baseline(field, args.log_n, 0, steps=args.steps)
     ms = 1000 * sum(times) / len(times)
     sample = (f"{cnt} x WinterfellFourStep {field.name} n=2^{args.log_n} forward (C restatement of "
-              f"src/encoders/winterfell_four_step.rs, OpenMP {cores} threads)")
+              f"src/encoders/winterfell_four_step.rs, OpenMP {cores} threads, gcc -O3 {flags})")
     line = {
         "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32" if field.word_bytes == 4 else "u64",
         "data": "synthetic (splitmix64 seed 42, uniform [0,p))",
-        "config": {"workload": f"{field.name} forward NTT n=2^{args.log_n}, batch 1",
-                   "field": field.name, "log_n": args.log_n, "batch": 1},
+        "config": workload_config(field, args.log_n),
         "impl": "reference",
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -464,10 +471,10 @@ def main():
     # ---- CPU baseline (rank 0, N=1 only): the oracle port on the host cores
     cpu = None
     if rank == 0 and world == 1:
-        cval, cores, cnt, _ = cpu_baseline(field, log_n, args.cpu_seconds)
+        cval, cores, cnt, _, flags = cpu_baseline(field, log_n, args.cpu_seconds)
         cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{cnt} x WinterfellFourStep {field.name} n=2^{log_n} forward, C restatement "
-                         f"of src/encoders/winterfell_four_step.rs, OpenMP {cores} threads"}
+                         f"of src/encoders/winterfell_four_step.rs, OpenMP {cores} threads, gcc -O3 {flags}"}
 
     # ---- CPU restatements of the reference's own encoders on the other configs
     # (rank 0, N=1): one bounded sample each, beside the GPU time of the same shape
@@ -482,11 +489,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32" if w == 4 else "u64",
             "data": "synthetic (splitmix64 seed 42+rank, uniform [0,p))",
-            "config": {"workload": f"{field.name} forward NTT n=2^{log_n}, batch 1 per GPU",
-                       "field": field.name, "log_n": log_n, "batch": 1,
-                       "plan": omr_ntt.plan_describe(field, log_n, plan),
-                       "l2": "flushed (256 MiB write) before every timed step",
-                       "parallelism": f"replicas x{world}"},
+            "config": workload_config(field, log_n),
+            "setup": {"plan": omr_ntt.plan_describe(field, log_n, plan),
+                      "l2": "flushed (256 MiB write) before every timed step",
+                      "parallelism": f"replicas x{world} (batch 1 per GPU)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": f"ntt_tile_pass pass {dom} (logT={passes[dom]['logT']})",

@@ -35,6 +35,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libntt_oracle.so")
+# the same sources built for the host CPU family (the timed CPU baseline)
+TUNED_PATH = os.path.join(HERE, "_build", "libntt_oracle_tuned.so")
 
 BABYBEAR, GOLDILOCKS, KOALABEAR, TEDDYBEAR = 0, 1, 2, 3
 FIELDS = {
@@ -80,12 +82,26 @@ def build() -> str:
     return LIB_PATH
 
 
+_use_tuned = False
+
+
+def use_tuned_build() -> str:
+    """Route every later call of this process through the CPU-tuned build
+    (bench.py's CPU-baseline and reference legs); returns its compiler flags."""
+    global _use_tuned, _lib
+    build()
+    _use_tuned, _lib = True, None
+    with open(os.path.join(HERE, "_build", "tune_flags.txt")) as fh:
+        return fh.read().strip()
+
+
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
+        path = TUNED_PATH if _use_tuned else LIB_PATH
+        if not os.path.exists(path):
             build()
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(path)
         L.oracle_ntt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64]
         L.oracle_ntt.restype = ctypes.c_int
         L.oracle_ntt_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32,

@@ -26,3 +26,10 @@ def test_reference_arm_prints_one_contract_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["e2e"]["value"] == d["value"]
+    # the same workload dict as the GPU arm prints, and the tuned CPU build named
+    sys.path.insert(0, ROOT)
+    import bench
+    from omr_ntt.fields import BabyBear
+
+    assert d["config"] == bench.workload_config(BabyBear, 16)
+    assert "gcc -O3 -m" in d["cpu_baseline"]["sample"]
