@@ -218,9 +218,12 @@ static int run_strategy_t(omr_ntt_domain_s* d, int strategy, int param, int patt
   const uint64_t n = d->n;
   switch (strategy) {
     case STRAT_DECOMP_:
-      if (pattern != OMR_NTT_PATTERN_PREFIX || count > 4096 || count >= n)
-        return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "decomposition serves prefixes of <= 4096 outputs");
-      return launch_prefix<F>(d, (uint32_t)count, param, in, out, stream);
+      if ((pattern != OMR_NTT_PATTERN_PREFIX && pattern != OMR_NTT_PATTERN_INDICES) || count > 4096 ||
+          count >= n)
+        return fail(OMR_NTT_ERR_INVALID_ARGUMENT,
+                    "decomposition serves prefixes and index sets of <= 4096 outputs");
+      return launch_prefix<F>(d, (uint32_t)count, param, in, out, stream,
+                              pattern == OMR_NTT_PATTERN_INDICES ? indices : nullptr);
     case STRAT_FOLD_:
       if (pattern != OMR_NTT_PATTERN_STRIDED || count >= n)
         return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "fold serves strided patterns");
@@ -250,8 +253,10 @@ int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uin
     return run_strategy_t<F>(d, strategy, param, pattern, count, indices, in, out, stream);
   if (pattern == OMR_NTT_PATTERN_STRIDED && count < n)
     return run_fold<F>(d, -1, count, in, out, stream);
-  if (pattern == OMR_NTT_PATTERN_PREFIX && count <= 4096 && count < n && n / count >= 2)
-    return launch_prefix<F>(d, (uint32_t)count, 0, in, out, stream);
+  if ((pattern == OMR_NTT_PATTERN_PREFIX || pattern == OMR_NTT_PATTERN_INDICES) && count <= 4096 &&
+      count < n && n / count >= 2)
+    return launch_prefix<F>(d, (uint32_t)count, 0, in, out, stream,
+                            pattern == OMR_NTT_PATTERN_INDICES ? indices : nullptr);
   return run_gather<F>(d, -1, pattern, count, indices, in, out, stream);
 }
 

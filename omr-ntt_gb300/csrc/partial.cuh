@@ -14,6 +14,8 @@
 //                      over CTAs (reads N words once, writes m).
 //   STRIDED s        : X[j N/s] = DFT_s(y)[j], y[n'] = sum_q x[n' + s q]
 //                      (fold N -> s by coset sums, then one s-point NTT).
+//   INDICES m <= 4096: the prefix decomposition with the index list:
+//                      X[j] = sum_r omega_N^{rj} Y_r[j mod T] for any j.
 //   otherwise        : full transform into scratch + gather.
 #pragma once
 #include "engine.cuh"

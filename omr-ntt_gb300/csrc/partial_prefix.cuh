@@ -26,6 +26,13 @@ namespace omr {
 // with no per-element twiddle lookups.  The slices are combined in shared
 // memory, one row of m words per CTA, and a row-reduction kernel sums the
 // rows.  The input is read once.
+//
+// The same sum serves any output index, not just a prefix: with M = N / T
+// columns, X[j] = sum_{r < M} omega_N^(r j) * Y_r[j mod T] for every j < N.
+// With an index list (idx != nullptr), output slot q < m is X[idx[q]]: its
+// tile row is idx[q] mod T and its Horner factor omega_N^(-TPK idx[q]) -- an
+// index-set request of m <= T outputs costs the prefix's work instead of a
+// full transform and a gather.
 template <class F, int LOGT>
 constexpr int prefix_cols() {  // ~64 KiB tile, rows of >= 16 bytes, <= 256 columns
   constexpr int lo = 16 / F::WORD;
@@ -84,7 +91,8 @@ constexpr size_t prefix_smem_bytes() {
 
 template <class F, int LOGT>
 __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
-    prefix_decomp_kernel(const PassArgs<F> a, uint32_t m, typename F::E* __restrict__ partial) {
+    prefix_decomp_kernel(const PassArgs<F> a, uint32_t m, const uint32_t* __restrict__ idx,
+                         typename F::E* __restrict__ partial) {
   using E = typename F::E;
   using Tw = typename F::Tw;
   constexpr int T = 1 << LOGT;
@@ -105,14 +113,21 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
   const uint32_t kbase = threadIdx.x % kact;
   const uint32_t slice = threadIdx.x / kact;
   const bool active = slice < tpk && kbase < m;
+  // output slot q is X[jq]: a prefix (jq = q) or an index list; its tile row
+  // is jq mod T
+  auto out_index = [&](uint32_t q) -> uint32_t { return idx ? idx[q] : q; };
+  // an index past N yields 0, as the gather of the full transform gives it
+  auto in_range = [&](uint32_t q) -> bool { return (uint64_t)out_index(q) <= (uint64_t)a.tw_mask; };
+  const uint32_t jb = active ? out_index(kbase) : 0u;
+  const int rowb = (int)(jb & (uint32_t)(T - 1));
 
   E acc = 0;
-  const Tw zi = omega_tw<F>(a, (uint64_t)0 - (uint64_t)tpk * kbase);  // omega_N^(-TPK k)
+  const Tw zi = omega_tw<F>(a, (uint64_t)0 - (uint64_t)tpk * jb);  // omega_N^(-TPK j)
   if constexpr (T > NT) {
     if (many)
       for (uint32_t k = threadIdx.x; k < m; k += NT) {  // this thread's outputs only
         acc_s[k] = 0;
-        zi_s[k] = omega_tw<F>(a, (uint64_t)0 - (uint64_t)k);
+        zi_s[k] = omega_tw<F>(a, (uint64_t)0 - (uint64_t)out_index(k));
       }
   }
 
@@ -128,8 +143,9 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
         for (uint32_t k = threadIdx.x; k < m; k += NT) {
           E h = acc_s[k];
           const Tw z = zi_s[k];
+          const int row = (int)(out_index(k) & (uint32_t)(T - 1));
 #pragma unroll
-          for (int c = 0; c < C; c++) h = F::add(F::mul_tw(h, z), s[tile_idx<F, C>((int)k, c)]);
+          for (int c = 0; c < C; c++) h = F::add(F::mul_tw(h, z), s[tile_idx<F, C>(row, c)]);
           acc_s[k] = h;
         }
       }
@@ -137,7 +153,7 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
     if (!many && active) {
 #pragma unroll 4
       for (uint32_t c = slice; c < (uint32_t)C; c += tpk)
-        acc = F::add(F::mul_tw(acc, zi), s[tile_idx<F, C>((int)kbase, (int)c)]);
+        acc = F::add(F::mul_tw(acc, zi), s[tile_idx<F, C>(rowb, (int)c)]);
     }
     __syncthreads();  // the next group's first round overwrites the tile
   }
@@ -146,13 +162,13 @@ __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
       const uint64_t r_last = (uint64_t)(g1 - 1) * C + (C - 1);
       for (uint32_t k = threadIdx.x; k < m; k += NT)
         partial[(uint64_t)blockIdx.x * m + k] =
-            g1 > g0 ? mul_m<F>(acc_s[k], omega_m<F>(a, r_last * k)) : (E)0;
+            g1 > g0 && in_range(k) ? mul_m<F>(acc_s[k], omega_m<F>(a, r_last * out_index(k))) : (E)0;
       return;
     }
   }
   if (g1 > g0 && active) {
     const uint64_t r_last = (uint64_t)(g1 - 1) * C + (C - tpk) + slice;
-    acc = mul_m<F>(acc, omega_m<F>(a, r_last * kbase));
+    acc = in_range(kbase) ? mul_m<F>(acc, omega_m<F>(a, r_last * jb)) : (E)0;
   }
   if (tpk > 1) {
     // combine the slices of every output: s[slice * kact + k]
@@ -219,8 +235,8 @@ inline int launch_reduce_rows(const typename F::E* partial, uint64_t rows, uint6
 }
 
 template <class F, int LOGT>
-inline int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void* out,
-                           cudaStream_t stream) {
+inline int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const uint32_t* idx, const void* in,
+                           void* out, cudaStream_t stream) {
   using E = typename F::E;
   using Tw = typename F::Tw;
   constexpr int T = 1 << LOGT;
@@ -262,14 +278,16 @@ inline int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const void* in, void
   void* part = nullptr;
   rc = domain_scratch(d, stream, (size_t)grid * m * sizeof(E), &part, 1);
   if (rc) return rc;
-  kern<<<grid, NT, smem, stream>>>(a, m, static_cast<E*>(part));
+  kern<<<grid, NT, smem, stream>>>(a, m, idx, static_cast<E*>(part));
   OMR_CUDA_TRY(cudaGetLastError());
   return launch_reduce_rows<F>(static_cast<const E*>(part), grid, m, static_cast<E*>(out), stream);
 }
 
+// m outputs: X[0..m) (idx == nullptr) or X[idx[q]] (device index list, every
+// idx[q] < N), line length 2^logt >= m (logt <= 0: the shortest).
 template <class F>
 int launch_prefix(omr_ntt_domain_s* d, uint32_t m, int logt, const void* in, void* out,
-                         cudaStream_t stream) {
+                  cudaStream_t stream, const uint32_t* idx) {
   if (logt <= 0) {
     logt = 0;
     while ((1u << logt) < m) logt++;
@@ -277,25 +295,29 @@ int launch_prefix(omr_ntt_domain_s* d, uint32_t m, int logt, const void* in, voi
   }
   if ((1u << logt) < m || (uint32_t)logt > d->log_n) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "decomposition line shorter than the prefix");
   switch (logt) {
-    case 1: return launch_prefix_t<F, 1>(d, m, in, out, stream);
-    case 2: return launch_prefix_t<F, 2>(d, m, in, out, stream);
-    case 3: return launch_prefix_t<F, 3>(d, m, in, out, stream);
-    case 4: return launch_prefix_t<F, 4>(d, m, in, out, stream);
-    case 5: return launch_prefix_t<F, 5>(d, m, in, out, stream);
-    case 6: return launch_prefix_t<F, 6>(d, m, in, out, stream);
-    case 7: return launch_prefix_t<F, 7>(d, m, in, out, stream);
-    case 8: return launch_prefix_t<F, 8>(d, m, in, out, stream);
-    case 9: return launch_prefix_t<F, 9>(d, m, in, out, stream);
-    case 10: return launch_prefix_t<F, 10>(d, m, in, out, stream);
-    case 11: return launch_prefix_t<F, 11>(d, m, in, out, stream);
-    case 12: return launch_prefix_t<F, 12>(d, m, in, out, stream);
+    case 1: return launch_prefix_t<F, 1>(d, m, idx, in, out, stream);
+    case 2: return launch_prefix_t<F, 2>(d, m, idx, in, out, stream);
+    case 3: return launch_prefix_t<F, 3>(d, m, idx, in, out, stream);
+    case 4: return launch_prefix_t<F, 4>(d, m, idx, in, out, stream);
+    case 5: return launch_prefix_t<F, 5>(d, m, idx, in, out, stream);
+    case 6: return launch_prefix_t<F, 6>(d, m, idx, in, out, stream);
+    case 7: return launch_prefix_t<F, 7>(d, m, idx, in, out, stream);
+    case 8: return launch_prefix_t<F, 8>(d, m, idx, in, out, stream);
+    case 9: return launch_prefix_t<F, 9>(d, m, idx, in, out, stream);
+    case 10: return launch_prefix_t<F, 10>(d, m, idx, in, out, stream);
+    case 11: return launch_prefix_t<F, 11>(d, m, idx, in, out, stream);
+    case 12: return launch_prefix_t<F, 12>(d, m, idx, in, out, stream);
   }
   return fail(OMR_NTT_ERR_SIZE, "prefix decomposition needs m <= 4096");
 }
 
-extern template int launch_prefix<BabyBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
-extern template int launch_prefix<Goldilocks>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
-extern template int launch_prefix<KoalaBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
-extern template int launch_prefix<TeddyBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t);
+extern template int launch_prefix<BabyBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t,
+                                        const uint32_t*);
+extern template int launch_prefix<Goldilocks>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t,
+                                        const uint32_t*);
+extern template int launch_prefix<KoalaBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t,
+                                        const uint32_t*);
+extern template int launch_prefix<TeddyBear>(omr_ntt_domain_s*, uint32_t, int, const void*, void*, cudaStream_t,
+                                        const uint32_t*);
 
 }  // namespace omr

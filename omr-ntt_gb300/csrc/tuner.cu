@@ -4,9 +4,10 @@
 // Its candidate plans are
 //   * full transforms  (count == N): every pass split x kernel variant of
 //     enumerate_plans (engine.cu);
-//   * partial outputs: the pruned prefix decomposition for each line length
-//     T >= count (T <= 4096), the strided fold + every plan of the count-point
-//     transform, and every full plan followed by a gather.
+//   * partial outputs: the pruned decomposition for each line length
+//     T >= count (T <= 4096; prefixes and index sets), the strided fold +
+//     every plan of the count-point transform, and every full plan followed
+//     by a gather.
 // omr_ntt_tune_point times every candidate on device buffers it owns (CUDA
 // events, L2 flushed before each timed run, median of `reps`); the caller
 // records the fastest in the planner database (omr_ntt_planner_*), which the
@@ -45,7 +46,7 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
     for (int p = 0; p < nfull; p++) v.push_back({STRAT_FULL, p});
     return v;
   }
-  if (pattern == OMR_NTT_PATTERN_PREFIX) {
+  if (pattern == OMR_NTT_PATTERN_PREFIX || pattern == OMR_NTT_PATTERN_INDICES) {
     int lt = 0;
     while ((1ull << lt) < count) lt++;
     if (lt == 0) lt = 1;
@@ -68,7 +69,7 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
 //           2: balanced with one more pass, 3: large-first (4096, ..., 4096, remainder);
 //           class 3 itself (plain tile pass, large-first: never the fastest
 //           on GB300) stands for the one-launch cluster plan of 2^13..2^16
-//   12..15  prefix decomposition with line length next_pow2(count) << j, j = 0..3
+//   12..15  decomposition (prefix or index set) with line length next_pow2(count) << j, j = 0..3
 //   16..27  strided fold, then the count-point transform with full class (c - 16)
 //   28..39  full transform with full class (c - 28), then gather
 constexpr int kNumClasses = 40;
@@ -121,7 +122,8 @@ static bool class_candidate(int field, uint32_t log_n, int pattern, uint64_t cou
   }
   if (full) return false;
   if (cls < 16) {
-    if (pattern != OMR_NTT_PATTERN_PREFIX || count > 4096) return false;
+    if ((pattern != OMR_NTT_PATTERN_PREFIX && pattern != OMR_NTT_PATTERN_INDICES) || count > 4096)
+      return false;
     int lt = 0;
     while ((1ull << lt) < count) lt++;
     if (lt == 0) lt = 1;

@@ -90,3 +90,27 @@ def test_strided_from_an_unaligned_pointer(oracle):
                                               ctypes.c_void_p(out.data_ptr()), None))
         torch.cuda.synchronize()
         assert np.array_equal(to_host(out, f.dtype), full[::n // s]), s
+
+
+@pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
+def test_index_set_decomposition_edges(oracle, field):
+    """Index sets run through the pruned decomposition: any order, repeated
+    indices, and an index past N (which yields 0, as the gather of the full
+    transform gives it), for small and large sets."""
+    import torch
+
+    n = 1 << 18
+    d = NttDomain(field, n)
+    x = gen_input_seeded(field, n, 31)
+    full = oracle.forward(field.id, x)
+    xd = to_dev(x)
+    rng = np.random.Generator(np.random.PCG64(5))
+    for m in (1, 7, 64, 1000, 4096):
+        idx = rng.integers(0, n, size=m).astype(np.uint32)  # unsorted, repeats
+        idx[m // 2] = idx[0]
+        if m > 1:
+            idx[-1] = n + 3  # past N
+        exp = np.where(idx < n, full[np.minimum(idx, n - 1).astype(np.int64)], 0).astype(field.dtype)
+        idt = torch.from_numpy(idx.view(np.int32)).cuda()
+        out = omr_ntt.partial(d, xd, INDICES, m, indices=idt)
+        assert np.array_equal(to_host(out, field.dtype), exp), m

@@ -43,6 +43,11 @@ def _cands(field, log_n, pattern, count):
     (BabyBear, 16, 0, 1 << 16, 3),
     (Goldilocks, 13, 0, 1 << 13, 2),
     (TeddyBear, 15, 0, 1 << 15, 2),
+    # index sets: the decomposition at every line length, then full + gather
+    (Goldilocks, 18, 2, 4096, 1),
+    (KoalaBear, 14, 2, 3, 1),
+    (TeddyBear, 16, 2, 1000, 2),
+    (BabyBear, 22, 2, 16, 1),
 ], ids=str)
 def test_all_candidates_agree(oracle, field, log_n, pattern, count, batch):
     import torch
