@@ -134,6 +134,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def pass_kernel(plan_name: str) -> str:
+    """The kernel that runs the passes of a plan (from its description)."""
+    for key, kern in (("wide", "ntt_wide_pass"), ("slab", "ntt_slab_pass"), ("cluster", "ntt_cluster_kernel"),
+                      ("tma", "ntt_tile_pass_tma")):
+        if key in plan_name:
+            return kern
+    return "ntt_tile_pass"
+
+
 def workload_config(field, log_n):
     """The `config` both arms print (the same workload, so the same dict)."""
     return {"workload": f"{field.name} forward NTT n=2^{log_n}, batch 1",
@@ -452,7 +461,7 @@ def main():
         net = lp.Mlp(seed=0)
         net.set_params(params)
         live = []
-        for p in pts[1500:1500 + 12]:
+        for p in pts[1500:1500 + 50]:
             ms = lp.tune(p, reps=3, seed=7)
             cm = lp.class_map(p)
             pred = net.forward(lp.features(p)[None])[0]
@@ -495,7 +504,8 @@ def main():
                       "parallelism": f"replicas x{world} (batch 1 per GPU)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": f"ntt_tile_pass pass {dom} (logT={passes[dom]['logT']})",
+                         "kernel": f"{pass_kernel(omr_ntt.plan_describe(field, log_n, plan))} pass {dom} "
+                                   f"(logT={passes[dom]['logT']})",
                          "peak_source": peak_src,
                          "pass_ms": [round(t, 4) for t in pass_ms],
                          "transform_frac": (2 * n * w / (ms_per_step / 1e3) / 1e9) / peak},

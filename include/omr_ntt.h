@@ -122,6 +122,17 @@ const char *omr_ntt_encoder_name(int encoder);
  * mirroring the reference's registry filter (src/encoders/mod.rs:39-44). */
 int omr_ntt_encoder_supports(int encoder, uint32_t log_n);
 
+/* The plan a full encoder runs for a 2^log_n transform of `field`: each of the
+ * reference's algorithms (src/encoders/*.rs) maps to the engine plan family
+ * with its structure -- WinterfellFourStep the balanced two-pass slab plan,
+ * Plonky3Radix2LayerSplit the shorter-pass-first split at log2(N) / 2,
+ * LambdaBowers the 256-point wide passes, LambdaRadix4 even-length passes,
+ * TfheStockhamRadix8 passes of a multiple of 3 bits on the Stockham tile
+ * pass, ArkRadix2 / Dft the planner's choice (also every family's fallback).
+ * All plans give the same words.  Returns the plan id, or a negative status
+ * (partial encoders, unsupported sizes).  No GPU needed. */
+int omr_ntt_encoder_plan(int encoder, int field, uint32_t log_n);
+
 /* NttEncoder::ntt(&self, buf, domain) (src/encoder.rs:71) on a device buffer:
  * in place on `batch` transforms of N words stored back to back.  Partial
  * encoders (DftPartial, TransformDecomposition, TransformDecompositionV2) use

@@ -2,6 +2,7 @@
 // encoders::all / all_partial) and the partial-output entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -25,13 +26,84 @@ static bool is_partial_encoder(int e) {
          e == OMR_NTT_TRANSFORM_DECOMPOSITION_V2;
 }
 
-// Plan family used for each full encoder: every plan computes the same
-// natural-order transform; the family only picks the pass split.  Four-step
-// style encoders take the balanced two/three-pass split, the radix-2 style
-// ones the planner's default.
+// The plan of the given pass split and kernel variant, or -1.
+static int find_plan(uint32_t log_n, const std::vector<int>& split, int variant) {
+  const auto& plans = plan_table(log_n);
+  for (int i = 0; i < (int)plans.size(); i++)
+    if (plans[i].variant == variant && plans[i].split == split) return i;
+  return -1;
+}
+// The first plan of the variant whose passes all satisfy `ok`, or -1.
+template <class Pred>
+static int find_plan_if(uint32_t log_n, int variant, Pred ok) {
+  const auto& plans = plan_table(log_n);
+  for (int i = 0; i < (int)plans.size(); i++)
+    if (plans[i].variant == variant && plans[i].split.size() > 1 &&
+        std::all_of(plans[i].split.begin(), plans[i].split.end(), ok))
+      return i;
+  return -1;
+}
+
+// Plan family of each full encoder.  Every plan computes the same
+// natural-order transform (so the words never depend on the encoder); the
+// family gives each of the reference's algorithms the engine plan that has
+// its structure:
+//   WinterfellFourStep (src/encoders/winterfell_four_step.rs:31-81): two
+//     factors near sqrt(N), row FFTs, twiddle, row FFTs -> the balanced
+//     two-pass split on the slab pass (which splits each line four-step
+//     style again: one stride-256 round, then 256-point slabs);
+//   Plonky3Radix2LayerSplit (src/encoders/plonky3_radix2_layer_split.rs:30-97):
+//     a DIT half and a Bowers half split at mid = log2(N) / 2 -> the split
+//     with the shorter pass first (floor(log N / 2), ceil(log N / 2)) on the
+//     double-buffered TMA pass;
+//   LambdaBowers (src/encoders/lambdaworks_bowers.rs:42-153): one DIF
+//     network with layers fused in pairs over the whole array -> the
+//     shortest-line family, the wide pass (256-point passes), on a split
+//     of 256-point passes only where there is one, else a split with a
+//     256-point pass;
+//   LambdaRadix4 (src/encoders/lambdaworks_radix4.rs:34-75): radix-4 stages
+//     only (even log N) -> a split into even-length passes on the two-CTA
+//     TMA pass;
+//   TfheStockhamRadix8 (src/encoders/tfhe_stockham_radix8.rs:80-140):
+//     radix-8 Stockham passes (log N % 3 == 0) -> a split into passes of a
+//     multiple of 3 bits on the plain Stockham tile pass;
+//   ArkRadix2, Dft and transforms that fit one pass (N <= 4096): the
+//     planner's choice.
+// A family without a plan at this size falls back to the planner's choice.
 static int encoder_plan(int encoder, int field, uint32_t log_n) {
-  (void)encoder;
-  return default_plan(field, log_n, 1);
+  const int dflt = default_plan(field, log_n, 1);
+  if (log_n <= (uint32_t)kMaxLogT) return dflt;
+  const int pmin = (int)((log_n + kMaxLogT - 1) / kMaxLogT);
+  std::vector<int> bal(pmin);
+  for (int i = 0; i < pmin; i++) bal[i] = (int)(log_n / pmin) + (i < (int)(log_n % pmin) ? 1 : 0);
+  int p = -1;
+  switch (encoder) {
+    case OMR_NTT_WINTERFELL_FOUR_STEP:
+      p = find_plan(log_n, bal, kSlabVariant);
+      break;
+    case OMR_NTT_PLONKY3_LAYER_SPLIT: {
+      std::vector<int> rev(bal.rbegin(), bal.rend());
+      p = find_plan(log_n, rev, 1);
+      break;
+    }
+    case OMR_NTT_LAMBDA_BOWERS: {
+      // all passes 256-point where the split allows it, else any wide plan
+      p = find_plan_if(log_n, kWideVariant, [](int t) { return t == 8; });
+      const auto& plans = plan_table(log_n);
+      for (int i = 0; p < 0 && i < (int)plans.size(); i++)
+        if (plans[i].variant == kWideVariant) p = i;
+      break;
+    }
+    case OMR_NTT_LAMBDA_RADIX4:
+      p = find_plan_if(log_n, 2, [](int t) { return t % 2 == 0; });
+      break;
+    case OMR_NTT_TFHE_STOCKHAM_R8:
+      p = find_plan_if(log_n, 0, [](int t) { return t % 3 == 0; });
+      break;
+    default:
+      break;
+  }
+  return p >= 0 ? p : dflt;
 }
 
 template <class F>
@@ -78,6 +150,16 @@ int omr_ntt_encoder_supports(int encoder, uint32_t log_n) {
   if (encoder == OMR_NTT_LAMBDA_RADIX4) return log_n % 2 == 0;
   if (encoder == OMR_NTT_TFHE_STOCKHAM_R8) return log_n % 3 == 0;
   return 1;
+}
+
+int omr_ntt_encoder_plan(int encoder, int field, uint32_t log_n) {
+  if (encoder < 0 || encoder >= kNumEncoders) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown encoder id");
+  if (!valid_field(field)) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "unknown field id");
+  if ((int)log_n > two_adicity(field)) return fail(OMR_NTT_ERR_SIZE, "log2(N) > TWO_ADICITY");
+  if (is_partial_encoder(encoder)) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "partial encoders run no full plan");
+  if (!omr_ntt_encoder_supports(encoder, log_n))
+    return fail(OMR_NTT_ERR_PRECONDITION, std::string(kEncoderNames[encoder]) + " does not support this size");
+  return encoder_plan(encoder, field, log_n);
 }
 
 int omr_ntt_encode(omr_ntt_domain_t d, int encoder, uint64_t s, void* buf, uint64_t batch,

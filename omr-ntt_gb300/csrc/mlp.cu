@@ -2,7 +2,7 @@
 // the GPU with hand-written kernels.
 //
 // Network: features (10) -> 64 -> ReLU -> 64 -> ReLU -> one score per plan
-// class (40, tuner.cu).  A score is the predicted log run time of the class
+// class (64, tuner.cu).  A score is the predicted log run time of the class
 // relative to the mean over the point's applicable classes; the selector
 // takes the applicable class with the lowest score.  Training minimises the
 // masked mean squared error against the autotuner's measured (centred) log

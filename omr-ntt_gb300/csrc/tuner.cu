@@ -64,26 +64,33 @@ static std::vector<Cand> candidates(int field, uint32_t log_n, int pattern, uint
 
 // ------------------------------------------------------------------ plan classes
 // A fixed, size-independent plan vocabulary for the learned planner:
-//   0..11   full transform: split kind x kernel variant 0..2 (class = 4 variant + kind);
+//   0..19   full transform: split kind x pass-kernel variant (class = 4 v + kind);
+//           v: 0 plain tile pass, 1 TMA double-buffered, 2 TMA two CTAs an SM,
+//           3 slab pass, 4 wide pass (256-point passes on 128-byte tiles);
 //           kind 0: balanced split with the fewest passes, 1: its reverse,
 //           2: balanced with one more pass, 3: large-first (4096, ..., 4096, remainder);
 //           class 3 itself (plain tile pass, large-first: never the fastest
 //           on GB300) stands for the one-launch cluster plan of 2^13..2^16
-//   12..15  decomposition (prefix or index set) with line length next_pow2(count) << j, j = 0..3
-//   16..27  strided fold, then the count-point transform with full class (c - 16)
-//   28..39  full transform with full class (c - 28), then gather
-constexpr int kNumClasses = 40;
+//   20..23  decomposition (prefix or index set) with line length next_pow2(count) << j, j = 0..3
+//   24..43  strided fold, then the count-point transform with full class (c - 24)
+//   44..63  full transform with full class (c - 44), then gather
+constexpr int kFullClasses = 20;
+constexpr int kDecompClass = kFullClasses, kFoldClass = kDecompClass + 4,
+              kGatherClass = kFoldClass + kFullClasses;
+constexpr int kNumClasses = kGatherClass + kFullClasses;
+constexpr int kClassVariant[5] = {0, 1, 2, kSlabVariant, kWideVariant};
 
-// plan id of full class fc (0..11) for a 2^log_n transform, or -1
+// plan id of full class fc (0..19) for a 2^log_n transform, or -1
 static int full_class_plan(uint32_t log_n, int fc) {
   const auto& plans = plan_table(log_n);
   if (log_n == 0) return fc == 0 ? 0 : -1;
+  if (fc < 0 || fc >= kFullClasses) return -1;
   if (fc == 3) {
     for (int i = 0; i < (int)plans.size(); i++)
       if (plans[i].variant == kClusterVariant) return i;
     return -1;
   }
-  const int variant = fc / 4, kind = fc % 4;
+  const int variant = kClassVariant[fc / 4], kind = fc % 4;
   const int pmin = std::max<int>(1, (int)((log_n + kMaxLogT - 1) / kMaxLogT));
   const int P = pmin + (kind == 2 ? 1 : 0);
   if ((uint32_t)P > log_n || P > 3) return -1;
@@ -113,7 +120,7 @@ static bool class_candidate(int field, uint32_t log_n, int pattern, uint64_t cou
   const uint64_t n = 1ull << log_n;
   const bool full = count >= n || count == 0;
   if (cls < 0 || cls >= kNumClasses) return false;
-  if (cls < 12) {
+  if (cls < kFullClasses) {
     if (!full) return false;
     int p = full_class_plan(log_n, cls);
     if (p < 0) return false;
@@ -121,27 +128,27 @@ static bool class_candidate(int field, uint32_t log_n, int pattern, uint64_t cou
     return true;
   }
   if (full) return false;
-  if (cls < 16) {
+  if (cls < kFoldClass) {
     if ((pattern != OMR_NTT_PATTERN_PREFIX && pattern != OMR_NTT_PATTERN_INDICES) || count > 4096)
       return false;
     int lt = 0;
     while ((1ull << lt) < count) lt++;
     if (lt == 0) lt = 1;
-    lt += cls - 12;
+    lt += cls - kDecompClass;
     if (lt > kMaxLogT || (uint32_t)lt >= log_n) return false;
     *out = Cand{STRAT_DECOMP, lt};
     return true;
   }
-  if (cls < 28) {
+  if (cls < kGatherClass) {
     if (pattern != OMR_NTT_PATTERN_STRIDED || (count & (count - 1))) return false;
     uint32_t ls = 0;
     while ((1ull << ls) < count) ls++;
-    int p = full_class_plan(ls, cls - 16);
+    int p = full_class_plan(ls, cls - kFoldClass);
     if (p < 0) return false;
     *out = Cand{STRAT_FOLD, p};
     return true;
   }
-  int p = full_class_plan(log_n, cls - 28);
+  int p = full_class_plan(log_n, cls - kGatherClass);
   if (p < 0) return false;
   *out = Cand{STRAT_GATHER, p};
   return true;
@@ -232,13 +239,20 @@ static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, ui
   return true;
 }
 
-// Built-in heuristic (measured on GB300): the one-launch cluster plan for
-// small or batched 2^13..2^16 transforms, else the TMA pass on the balanced
-// split (two CTAs per SM for the 32-bit fields, double-buffered for
-// Goldilocks), else plan 0.
+// Built-in heuristic (measured on GB300): the wide pass where a transform
+// splits into 256-point passes only (2^24 = 256^3, and batches of 2^16 =
+// 256^2; one 2^16 transform is latency bound and takes the cluster plan),
+// the one-launch cluster plan for small or batched 2^13..2^16 transforms,
+// else the TMA pass on the balanced split (two CTAs per SM for the 32-bit
+// fields, double-buffered for Goldilocks), else plan 0.
 static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   const auto& plans = plan_table(log_n);
   if (plans.size() <= 1 || plans[0].split.size() < 2) return 0;
+  if (log_n == 24 || (log_n == 16 && batch >= 8))
+    for (int i = 0; i < (int)plans.size(); i++)
+      if (plans[i].variant == kWideVariant &&
+          std::all_of(plans[i].split.begin(), plans[i].split.end(), [](int t) { return t == 8; }))
+        return i;
   // the one-launch cluster plan wins where latency dominates: up to 2^14, or
   // batches of 8 and more (one cluster per transform)
   if (log_n <= 14 || batch >= 8)

@@ -46,6 +46,7 @@ _SIGS = {
     "omr_ntt_domain_twiddles": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_void_p]),
     "omr_ntt_encoder_name": (_c.c_char_p, [_c.c_int]),
     "omr_ntt_encoder_supports": (_c.c_int, [_c.c_int, _c.c_uint32]),
+    "omr_ntt_encoder_plan": (_c.c_int, [_c.c_int, _c.c_int, _c.c_uint32]),
     "omr_ntt_encode": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_uint64, _c.c_void_p, _c.c_uint64,
                                    _c.c_void_p]),
     "omr_ntt_encode_host": (_c.c_int, [_c.c_void_p, _c.c_int, _c.c_uint64, _c.c_void_p, _c.c_uint64]),

@@ -46,6 +46,14 @@ class NttEncoder:
     def supports(self, log_n: int) -> bool:
         return bool(lib().omr_ntt_encoder_supports(self.ID, log_n))
 
+    def plan(self, field, log_n: int) -> int:
+        """The engine plan this (full) encoder runs at 2^log_n: the plan
+        family with the structure of the reference algorithm."""
+        rc = lib().omr_ntt_encoder_plan(self.ID, field.id, log_n)
+        if rc < 0:
+            check(rc)
+        return rc
+
     def __repr__(self):
         return self.name() if self.s == 0 else f"{self.name()}({self.s})"
 

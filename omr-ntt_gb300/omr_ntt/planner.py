@@ -2,7 +2,7 @@
 
 A planning point is (field, log2 n, log2 s, output pattern, batch).  The
 exhaustive autotuner (omr_ntt_tune_point, native) times every candidate plan
-of the point; the 40 plan classes (omr_ntt_plan_class_candidate) give a fixed
+of the point; the 64 plan classes (omr_ntt_plan_class_candidate) give a fixed
 output vocabulary for the network.  The network (omr_ntt_mlp_*, trained on
 the GPU by the library's own kernels) predicts each applicable class's log
 time relative to the point's mean; its choice is the lowest prediction.
@@ -194,13 +194,28 @@ def choose(pred, T):
     return masked.argmin(1)
 
 
+# class layout (tuner.cu): 20 full-transform classes (4 x pass-kernel variant
+# + split kind), 4 decomposition classes, 20 fold classes, 20 gather classes
+FULL_CLASSES = 20
+DECOMP_CLASS = FULL_CLASSES
+FOLD_CLASS = DECOMP_CLASS + 4
+GATHER_CLASS = FOLD_CLASS + FULL_CLASSES
+
+
 def heuristic_class(p) -> int:
     """The class the planner picks without database or network (its built-in
-    rule): tuned TMA kernel on the balanced split for the headline fields,
-    decomposition for prefixes <= 4096, fold for strided sets, else gather."""
+    rule, tuner.cu heuristic_full_plan and partial.cu partial_dispatch): the
+    wide pass where the transform splits into 256-point passes only (2^24;
+    batches of 2^16), the cluster plan for small or batched 2^13..2^16, else
+    the tuned TMA pass on the balanced split; the decomposition for prefixes
+    and index sets <= 4096, the fold for strided sets, else the gather."""
     tma_cls = {0: 8, 1: 4}  # BabyBear: two CTAs per SM; Goldilocks: double-buffered
 
     def full_class(log_n, batch):
+        if log_n == 24:
+            return 4 * 4 + 2  # wide pass, 256 x 256 x 256 (one pass more than the fewest)
+        if log_n == 16 and batch >= 8:
+            return 4 * 4 + 0  # wide pass, 256 x 256
         if 13 <= log_n <= 16 and (log_n <= 14 or batch >= 8):
             return 3  # the one-launch cluster plan
         return tma_cls[p["field"]] if (log_n > 12 and p["field"] in (0, 1)) else 0
@@ -210,11 +225,10 @@ def heuristic_class(p) -> int:
     if s >= n:
         return full_cls
     if p["pattern"] == "strided":
-        sub_full = full_class(p["log_s"], 1)
-        return 16 + sub_full
-    if p["pattern"] == "contiguous" and s <= 4096 and n // s >= 2:
-        return 12
-    return 28 + full_class(p["log_n"], 1)  # the gather runs one transform at a time
+        return FOLD_CLASS + full_class(p["log_s"], 1)
+    if p["pattern"] in ("contiguous", "random") and s <= 4096 and n // s >= 2:
+        return DECOMP_CLASS
+    return GATHER_CLASS + full_class(p["log_n"], 1)  # the gather runs one transform at a time
 
 
 def regret(T, best, choice):

@@ -75,6 +75,35 @@ def test_all_registry_at_2_24(oracle):
         assert np.array_equal(to_host(buf, BabyBear.dtype), expected), enc.name()
 
 
+FAMILY = {"WinterfellFourStep": "slab", "Plonky3Radix2LayerSplit": "tma2buf",
+          "LambdaBowers": "wide", "LambdaRadix4": "tma2cta", "TfheStockhamRadix8": "tile"}
+
+
+@pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
+def test_encoder_plan_families_agree(oracle, field):
+    """Each reference algorithm runs its own plan family (its structure in
+    engine plans) and every family gives the oracle's words."""
+    import omr_ntt
+
+    for log_n in (16, 18, 20, 21, 22, 24):
+        n = 1 << log_n
+        domain = NttDomain(field, n)
+        inp = gen_input_seeded(field, n, 100 + log_n)
+        expected = oracle.forward(field.id, inp)
+        xd = to_dev(inp)
+        for enc in (WinterfellFourStep(), Plonky3Radix2LayerSplit(), LambdaBowers(), LambdaRadix4(),
+                    TfheStockhamRadix8()):
+            if not enc.supports(log_n):
+                continue
+            name = omr_ntt.plan_describe(field, log_n, enc.plan(field, log_n))
+            # LambdaBowers has a wide plan where a split has a 256-point pass
+            if enc.name() != "LambdaBowers" or log_n in (16, 20, 22, 24):
+                assert FAMILY[enc.name()] in name, (enc.name(), log_n, name)
+            buf = xd.clone()
+            enc.ntt(buf, domain)
+            assert np.array_equal(to_host(buf, field.dtype), expected), (enc.name(), log_n, name)
+
+
 @pytest.mark.parametrize("s", [2, 4, 8, 16, 50])
 def test_dft_partial_agrees_with_ark(oracle, s):
     assert_prefix_agrees_with_ark(oracle, DftPartial(s), s, [64, 128, 256])

@@ -24,8 +24,9 @@ def test_candidate_families():
     assert (1, 6) in pre and (1, 12) in pre and any(s == 3 for s, _ in pre)
     strided = cands(Goldilocks, 22, 1, 1024)
     assert any(s == 2 for s, _ in strided) and any(s == 3 for s, _ in strided)
-    rnd = cands(BabyBear, 20, 2, 100)
-    assert all(s == 3 for s, _ in rnd)
+    rnd = cands(BabyBear, 20, 2, 100)  # index sets: the decomposition, or full + gather
+    assert (1, 7) in rnd and (1, 12) in rnd and any(s == 3 for s, _ in rnd)
+    assert all(s in (1, 3) for s, _ in rnd)
     # the planning space of the learned selector: tens of plans per point
     assert 10 <= len(pre) <= 60
 
@@ -45,3 +46,26 @@ def test_planner_db_roundtrip(tmp_path):
     assert L.omr_ntt_planner_get(1, 22, 1, 0, 256, ctypes.byref(s), ctypes.byref(p)) == 1
     assert (s.value, p.value) == (1, 9)
     L.omr_ntt_planner_clear()
+
+
+def test_encoder_plan_families_are_distinct():
+    """The reference's full encoders map to distinct engine plan families
+    (no GPU needed): at 2^24 five different plans, each named for its family."""
+    import omr_ntt
+    from omr_ntt import encoders as E
+
+    fams = {"WinterfellFourStep": "4096x4096 slab", "Plonky3Radix2LayerSplit": "4096x4096 tma2buf",
+            "LambdaBowers": "256x256x256 wide", "LambdaRadix4": "4096x4096 tma2cta",
+            "TfheStockhamRadix8": "4096x4096 tile"}
+    plans = {}
+    for enc in (E.WinterfellFourStep(), E.Plonky3Radix2LayerSplit(), E.LambdaBowers(), E.LambdaRadix4(),
+                E.TfheStockhamRadix8()):
+        p = enc.plan(BabyBear, 24)
+        assert omr_ntt.plan_describe(BabyBear, 24, p).endswith(fams[enc.name()]), enc.name()
+        plans[enc.name()] = p
+    assert len(set(plans.values())) == 5
+    # the radix-4 family keeps to even-length passes where the balanced split is odd
+    assert omr_ntt.plan_describe(BabyBear, 22, E.LambdaRadix4().plan(BabyBear, 22)).endswith("1024x4096 tma2cta")
+    # one-pass sizes and the partial encoders
+    assert E.WinterfellFourStep().plan(BabyBear, 12) == E.ArkRadix2().plan(BabyBear, 12)
+    assert L.omr_ntt_encoder_plan(7, 0, 20) < 0 and L.omr_ntt_encoder_plan(4, 0, 21) < 0
