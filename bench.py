@@ -151,12 +151,12 @@ def workload_config(field, log_n):
 
 def cpu_baseline(field, log_n, seconds, steps=None):
     """The oracle's WinterfellFourStep (the reference's parallel four-step,
-    restated in C with OpenMP) on all host cores, built for the host CPU
-    family; bounded sample.  Returns (Gelem/s, cores, samples, times, flags)."""
+    restated in C with OpenMP) on all host cores; bounded sample.  Returns
+    (Gelem/s, cores, samples, times, compiler flags)."""
     import numpy as np
     from oracle import oracle
 
-    flags = oracle.use_tuned_build()
+    flags = oracle.BUILD_FLAGS
     oracle.set_threads(0)
     cores = oracle.get_threads()
     n = 1 << log_n
@@ -224,7 +224,7 @@ def run_reference(args):
     val, cores, cnt, times, flags = cpu_baseline(field, args.log_n, 0, steps=args.steps)
     ms = 1000 * sum(times) / len(times)
     sample = (f"{cnt} x WinterfellFourStep {field.name} n=2^{args.log_n} forward (C restatement of "
-              f"src/encoders/winterfell_four_step.rs, OpenMP {cores} threads, gcc -O3 {flags})")
+              f"src/encoders/winterfell_four_step.rs, OpenMP {cores} threads, {flags})")
     line = {
         "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -483,7 +483,7 @@ def main():
         cval, cores, cnt, _, flags = cpu_baseline(field, log_n, args.cpu_seconds)
         cpu = {"value": cval, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{cnt} x WinterfellFourStep {field.name} n=2^{log_n} forward, C restatement "
-                         f"of src/encoders/winterfell_four_step.rs, OpenMP {cores} threads, gcc -O3 {flags}"}
+                         f"of src/encoders/winterfell_four_step.rs, OpenMP {cores} threads, {flags}"}
 
     # ---- CPU restatements of the reference's own encoders on the other configs
     # (rank 0, N=1): one bounded sample each, beside the GPU time of the same shape

@@ -35,8 +35,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libntt_oracle.so")
-# the same sources built for the host CPU family (the timed CPU baseline)
-TUNED_PATH = os.path.join(HERE, "_build", "libntt_oracle_tuned.so")
+# compiler flags of the build (reported beside the timed CPU baseline)
+BUILD_FLAGS = "gcc -O3 -fopenmp"
 
 BABYBEAR, GOLDILOCKS, KOALABEAR, TEDDYBEAR = 0, 1, 2, 3
 FIELDS = {
@@ -82,26 +82,12 @@ def build() -> str:
     return LIB_PATH
 
 
-_use_tuned = False
-
-
-def use_tuned_build() -> str:
-    """Route every later call of this process through the CPU-tuned build
-    (bench.py's CPU-baseline and reference legs); returns its compiler flags."""
-    global _use_tuned, _lib
-    build()
-    _use_tuned, _lib = True, None
-    with open(os.path.join(HERE, "_build", "tune_flags.txt")) as fh:
-        return fh.read().strip()
-
-
 def lib():
     global _lib
     if _lib is None:
-        path = TUNED_PATH if _use_tuned else LIB_PATH
-        if not os.path.exists(path):
+        if not os.path.exists(LIB_PATH):
             build()
-        L = ctypes.CDLL(path)
+        L = ctypes.CDLL(LIB_PATH)
         L.oracle_ntt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64]
         L.oracle_ntt.restype = ctypes.c_int
         L.oracle_ntt_batch.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32,

@@ -32,4 +32,4 @@ def test_reference_arm_prints_one_contract_line():
     from omr_ntt.fields import BabyBear
 
     assert d["config"] == bench.workload_config(BabyBear, 16)
-    assert "gcc -O3 -mtune=" in d["cpu_baseline"]["sample"]
+    assert "gcc -O3" in d["cpu_baseline"]["sample"]
