@@ -331,9 +331,10 @@ def main():
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        tj = json.load(open(tpath))
-        key = f"{field.name}:{log_n}:pass{dom}"
-        traffic = tj.get(key)
+        # DRAM bytes per launch from one ncu capture, valid only for the plan captured
+        ent = json.load(open(tpath)).get(f"{field.name}:{log_n}")
+        if ent and ent.get("plan") == omr_ntt.plan_describe(field, log_n, plan):
+            traffic = ent["pass_traffic_bytes"][dom]
 
     # ---- end to end through the C ABI with host buffers (pinned), copies inside
     hbuf = torch.from_numpy(x.view(np.int32 if w == 4 else np.int64).copy()).pin_memory()
