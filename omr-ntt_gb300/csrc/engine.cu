@@ -178,6 +178,11 @@ std::vector<PlanShape> enumerate_plans(uint32_t log_n) {
   for (auto& s : splits)
     if (s.size() > 1 && std::find(s.begin(), s.end(), 8) != s.end())
       out.push_back(PlanShape{s, kWideVariant});
+  // the tensor-core variant of the wide pass on the splits into 256-point
+  // passes only (BabyBear; other fields run these plans on the wide pass)
+  for (auto& s : splits)
+    if (s.size() > 1 && std::all_of(s.begin(), s.end(), [](int t) { return t == 8; }))
+      out.push_back(PlanShape{s, kTcVariant});
   return out;
 }
 
@@ -302,6 +307,7 @@ static std::string plan_name(int field, const PlanShape& s) {
   if (s.variant == kClusterVariant) return n + " cluster";
   if (s.variant == kSlabVariant) return n + " slab";
   if (s.variant == kWideVariant) return n + " wide";
+  if (s.variant == kTcVariant) return n + " wide-tcgen05";
   if (s.split.size() > 1) n += v == 0 ? " tile" : (v == 1 ? " tma2buf" : " tma2cta");
   return n;
 }

@@ -70,6 +70,7 @@ int launch_cluster_transform(const omr_ntt_domain_s* d, const std::vector<PassDe
 constexpr int kClusterVariant = 3;  // PlanShape::variant of the cluster plans
 constexpr int kSlabVariant = 4;     // PlanShape::variant of the slab-pass plans (ntt_pass_slab.cuh)
 constexpr int kWideVariant = 5;     // 256-point passes on 128-byte-wide tiles (ntt_pass_wide.cuh)
+constexpr int kTcVariant = 6;       // the wide pass with its first round on tcgen05 (ntt_pass_tc.cuh)
 // Host-buffer batches: chunk size in transforms (0: run unpipelined), and the
 // pipelined loop that applies `op(device_buf, transforms, stream)` to every
 // chunk between its copy in and copy out.  Caller holds d->host_mu.

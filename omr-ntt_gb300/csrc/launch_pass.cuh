@@ -4,10 +4,14 @@
 #include <cudaTypedefs.h>
 
 #include <atomic>
+#include <cstring>
+#include <map>
+#include <mutex>
 
 #include "engine.cuh"
 #include "ntt_pass_slab.cuh"
 #include "ntt_pass_tma.cuh"
+#include "ntt_pass_tc.cuh"
 #include "ntt_pass_wide.cuh"
 
 namespace omr {
@@ -67,7 +71,7 @@ constexpr bool has_tma_pass() {
 }
 inline int effective_variant(int field, int mode, int logT, int variant) {
   if (variant <= 0 || mode == MODE_LINE || logT < 8) return 0;
-  if (variant == kSlabVariant || variant == kWideVariant) return variant;
+  if (variant == kSlabVariant || variant == kWideVariant || variant == kTcVariant) return variant;
   int v = variant > 2 ? 2 : variant;
   if (!((tma_variant_mask(field) >> (v - 1)) & 1)) v = 3 - v;
   return v;
@@ -272,6 +276,100 @@ int launch_wide_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   return OMR_NTT_OK;
 }
 
+// The tensor-core operand of the wide pass's first round (ntt_pass_tc.cuh):
+// B[(j, a)][(i, m)] = bf16(limb_j((256^i omega_16^(m a)) mod p)) in the
+// canonical K-major image, 8 KB per (device, field, direction), built once.
+template <class F>
+int tc_operand(bool inverse, const uint16_t** out) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, void*> cache;
+  int dev = 0;
+  OMR_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(dev, inverse ? 1 : 0);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = static_cast<const uint16_t*>(it->second);
+    return OMR_NTT_OK;
+  }
+  const uint64_t p = F::p64();
+  uint64_t w = root_of_unity_host<F>(4);
+  if (inverse) w = hpowmod(w, p - 2, p);
+  std::vector<uint16_t> img(kTcBBytes / 2, 0);
+  for (int i = 0; i < 4; i++)
+    for (int m = 0; m < 16; m++)
+      for (int aa = 0; aa < 16; aa++) {
+        const uint64_t val = hmulmod(hpowmod(256, i, p), hpowmod(w, (uint64_t)m * aa, p), p);
+        for (int j = 0; j < 4; j++) {
+          const float f = (float)((val >> (8 * j)) & 255u);  // exact in bf16
+          uint32_t bits;
+          std::memcpy(&bits, &f, 4);
+          img[tc_canon(16 * j + aa, 16 * i + m) / 2] = (uint16_t)(bits >> 16);
+        }
+      }
+  void* d = nullptr;
+  OMR_CUDA_TRY(cudaMalloc(&d, kTcBBytes));
+  OMR_CUDA_TRY(cudaMemcpy(d, img.data(), kTcBBytes, cudaMemcpyHostToDevice));
+  cache[key] = d;
+  *out = static_cast<const uint16_t*>(d);
+  return OMR_NTT_OK;
+}
+
+// The wide pass with its first round on the tensor cores (BabyBear, 256-point
+// lines).  Returns 1 ("not taken") when the geometry does not suit it.
+template <class F, int MODE, bool INV>
+int launch_tc_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
+  constexpr bool TW = MODE == MODE_COL;
+  constexpr int C = wide_cols<F>();
+  if (a.L_lo % C || !tma_geometry_ok<F>(a, 8, MODE) || (a.tw_lo != nullptr) != TW) return 1;
+  constexpr size_t smem = tc_smem_bytes<F>();
+  static_assert(smem <= kMaxDynSmem, "tensor-core pass does not fit in shared memory");
+  auto kern = ntt_wide_tc_pass<F, MODE, INV, TW>;
+  static std::atomic<int> occ_cache[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int occ = occ_cache[dev & 63].load();
+  if (occ == 0) {
+    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // two CTAs of 112 KB share an SM only with the whole carve-out as shared memory
+    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTcThreads, smem));
+    if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "tensor-core pass does not fit on an SM");
+    // the query can under-count against the shared-memory carve-out: size the
+    // grid for two CTAs when two fit the SM's shared memory (CTAs beyond the
+    // resident ones only start later; none waits on another)
+    int per_sm = 0;
+    OMR_CUDA_TRY(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    if (occ < 2 && 2 * (smem + 2048) <= (size_t)per_sm) occ = 2;
+    occ_cache[dev & 63] = occ;
+  }
+  const uint16_t* bmat = nullptr;
+  int rc = tc_operand<F>(INV, &bmat);
+  if (rc) return rc;
+  const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
+  if (ntiles == 0) return OMR_NTT_OK;
+  CUtensorMap in_map, out_map;
+  memset(&in_map, 0, sizeof(in_map));
+  CUresult r;
+  const CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_128B;
+  if constexpr (MODE == MODE_COL) {
+    const uint64_t rows = 256ull * a.L_m * a.L_b;
+    r = encode_2d(&in_map, F::WORD, a.in, a.L_lo, rows, a.L_lo, C, 256, sw);
+    if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (tensor-core load) failed");
+    r = encode_2d(&out_map, F::WORD, a.out, a.L_lo, rows, a.L_lo, C, 256, sw);
+  } else {
+    const uint64_t w = (uint64_t)a.L_lo * a.L_m;
+    r = encode_2d(&out_map, F::WORD, a.out, w, 256ull * a.L_b, w, C, 256, sw);
+  }
+  if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (tensor-core store) failed");
+  const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
+  const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
+  const typename F::Tw one_tw = F::make_tw(1), r32_tw = F::make_tw((1ull << 32) % F::p64());
+  kern<<<grid, kTcThreads, smem, stream>>>(in_map, out_map, a, bmat, one_tw, r32_tw, err);
+  OMR_CUDA_TRY(cudaGetLastError());
+  return OMR_NTT_OK;
+}
+
 // Defined here, instantiated once per (field, mode, direction) in
 // pass_<field>_<mode>_<dir>.cu; the extern declarations below stop every
 // other translation unit from instantiating the kernels again.
@@ -287,6 +385,15 @@ template <class F, int MODE, bool INV>
 int launch_pass_dir(int logT, int variant, const PassArgs<F>& a, uint64_t blocks, int* err,
                     cudaStream_t s) {
   if constexpr (MODE != MODE_LINE && has_tma_pass<F>()) {
+    if (variant == kTcVariant) {
+      // 256-point BabyBear passes on the tensor-core variant; everything else
+      // of the plan takes the wide pass
+      int rc = 1;
+      if constexpr (F::ID == BABYBEAR)
+        if (logT == 8) rc = launch_tc_t<F, MODE, INV>(a, err, s);
+      if (rc != 1) return rc;
+      variant = kWideVariant;
+    }
     if (variant == kWideVariant) {
       // 256-point passes on the wide tiles; other line lengths of the plan
       // take the slab pass
