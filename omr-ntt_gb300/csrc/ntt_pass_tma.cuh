@@ -45,6 +45,18 @@ OMR_D void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
                "r"(bytes)
                : "memory");
 }
+// Programmatic dependent launch: a pass launched with the programmatic
+// stream-serialisation attribute may start while the previous kernel of the
+// stream finishes; griddepcontrol.wait blocks until that kernel has completed
+// and its writes are visible, launch_dependents lets the next one start.
+OMR_D void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+OMR_D void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+OMR_D void prefetch_tmap(const CUtensorMap* m) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
+}
+OMR_D void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 OMR_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -302,6 +314,13 @@ template <class F, int C>
 OMR_D void tile_coords(const PassArgs<F>& a, uint64_t tile, uint32_t& g, uint32_t& lm,
                        uint64_t& lb) {
   const uint32_t groups = (a.L_lo + C - 1) / C;
+  if (tile >> 32 == 0) {  // 32-bit divisions (a fraction of the 64-bit ones' cost)
+    const uint32_t t = (uint32_t)tile, rest = t / groups;
+    g = t - rest * groups;
+    lm = rest % a.L_m;
+    lb = rest / a.L_m;
+    return;
+  }
   g = (uint32_t)(tile % groups);
   const uint64_t rest = tile / groups;
   lm = (uint32_t)(rest % a.L_m);

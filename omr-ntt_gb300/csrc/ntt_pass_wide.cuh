@@ -129,6 +129,29 @@ OMR_D void wide_issue_store(const CUtensorMap* map, const PassArgs<F>& a, uint64
   bulk_commit();
 }
 
+// wide_issue_load by a whole warp: the row passes' C line copies go out
+// from C lanes at once (one thread issues a bulk copy in ~70 ns, so C = 32
+// copies from one thread take longer than the tile's compute).  The
+// expect-tx arrive (lane 0) comes first; column passes are one TMA load.
+template <class F, int MODE>
+OMR_D void wide_issue_load_warp(const CUtensorMap* map, const PassArgs<F>& a, uint64_t tile,
+                                unsigned char* buf, uint64_t* bar, int lane) {
+  using E = typename F::E;
+  constexpr int C = wide_cols<F>();
+  if constexpr (MODE == MODE_COL) {
+    if (lane == 0) wide_issue_load<F, MODE>(map, a, tile, buf, bar);
+  } else {
+    uint32_t g, lm;
+    uint64_t lb;
+    tile_coords<F, C>(a, tile, g, lm, lb);
+    if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)(256 * C * F::WORD));
+    __syncwarp();
+    const E* src = a.in + (lb * a.is_b + lm * a.is_m + (uint64_t)(g * C) * a.is_lo);
+    if (lane < C)
+      bulk_load(buf + lane * wide_line_bytes<F>(), src + (uint64_t)lane * a.is_lo, 256 * F::WORD, bar);
+  }
+}
+
 // One warp: the 256-point transforms of column group w.  The results are
 // left in registers, v[c][b] = line entry a + 16 b (a = lane & 15); column
 // passes also write them to the swizzled rows in place, row passes re-lay
@@ -228,6 +251,8 @@ __global__ void __launch_bounds__(kWideThreads, 3)  // shared memory holds three
   const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
   uint64_t tile = blockIdx.x;
   if (threadIdx.x == 0) {
+    prefetch_tmap(&in_map);
+    prefetch_tmap(&out_map);
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
     fence_mbar_init();
@@ -237,6 +262,9 @@ __global__ void __launch_bounds__(kWideThreads, 3)  // shared memory holds three
   __syncthreads();
   uint32_t outstanding = 0;  // bit b: a load into buffer b has not been waited for
   if (threadIdx.x == 0) {
+    // the previous pass's output is this one's input (and its input may be
+    // this one's output): every global access of the pass follows this wait
+    grid_dep_wait();
     if (tile < ntiles) {
       wide_issue_load<F, MODE>(&in_map, a, tile, base, &bars[0]);
       outstanding |= 1u;
@@ -246,6 +274,7 @@ __global__ void __launch_bounds__(kWideThreads, 3)  // shared memory holds three
       outstanding |= 2u;
     }
   }
+  grid_dep_launch();
   for (int i = threadIdx.x; i < 15 * 16; i += kWideThreads) {
     const int aa = i / 16 + 1, l = i % 16;
     tab1[i] = a.roots[(uint32_t)(l * aa) * a.roots_stride];  // omega_256^(l a)
@@ -297,6 +326,194 @@ __global__ void __launch_bounds__(kWideThreads, 3)  // shared memory holds three
     bulk_wait_all();
     for (int bb = 0; bb < 2; bb++)
       if ((outstanding >> bb) & 1) mbar_wait_bounded(&bars[bb], (phase >> bb) & 1);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The same pass as one warp-specialised CTA per SM.  kWideSlots tile buffers
+// cycle through load -> compute -> store: a loader warp issues the TMA loads,
+// 24 consumer warps claim units (tile j, column group w) in order from a
+// shared counter, so the eight column groups of a tile run on eight warps at
+// once and every warp stays busy until the CTA's last unit, and a storer warp
+// issues each tile's TMA store and hands the buffer back.  No CTA barrier:
+// per buffer slot, `full` completes when the tile has landed, `done` when its
+// eight units are written back, `empty` when its store has read it, and for
+// row passes `rd` when its eight units have read their lines (the lines are
+// re-laid as rows in place).
+//
+// Units are claimed in order but finish in any order, so a consumer can be
+// more than one use of its slot ahead of the loads (a slow warp holding a
+// unit of tile j - kWideSlots keeps that slot from being refilled while
+// others run on).  A parity wait alone would then see an old phase as done:
+// the producer publishes which tile each slot holds (`slot_tile`) before it
+// issues the load, and a consumer waits for its tile to be the slot's before
+// it waits on `full`.  `rd` and `done` are safe without that check, because
+// a unit reaches them only after its tile's load, i.e. after every unit of
+// the slot's previous tile has passed both.
+constexpr int kWideConsumers = 24;
+constexpr int kWideWsThreads = 32 * (kWideConsumers + 2);  // + loader and storer warps
+constexpr int kWideSlots = 6;
+
+template <class F>
+constexpr size_t wide_ws_smem_bytes() {
+  return kWideSlots * (size_t)wide_buf_bytes<F>() + 15 * 16 * sizeof(typename F::Tw) + 1024;
+}
+
+template <class F, int MODE, bool INV, bool TW>
+__global__ void __launch_bounds__(kWideWsThreads, 1)
+    ntt_wide_ws_pass(const __grid_constant__ CUtensorMap in_map,
+                     const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
+  using E = typename F::E;
+  using Tw = typename F::Tw;
+  constexpr int C = wide_cols<F>(), VPU = slab_vpu<F>(), S = kWideSlots;
+  constexpr int BB = wide_buf_bytes<F>();
+  extern __shared__ __align__(1024) unsigned char wide_ws_smem_raw[];
+  __shared__ __align__(8) uint64_t full[S], done[S], rd[S], empty[S];
+  __shared__ uint32_t unit_next;
+  __shared__ volatile uint32_t slot_tile[S];  // j of the load last issued into each slot
+  __shared__ volatile int abort_flag;
+  unsigned char* base = wide_ws_smem_raw + ((1024u - (smem_u32(wide_ws_smem_raw) & 1023u)) & 1023u);
+  Tw* tab1 = reinterpret_cast<Tw*>(base + S * BB);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // this CTA's tiles: blockIdx.x + j * gridDim.x, j < njobs
+  const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
+  const uint32_t njobs =
+      ntiles > blockIdx.x ? (uint32_t)((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x) : 0u;
+  auto tile_of = [&](uint32_t j) { return blockIdx.x + (uint64_t)j * gridDim.x; };
+
+  // The loader warp sets up the barriers and sends the first loads before
+  // anything else, so the copies overlap the table setup.
+  const bool loader = warp == kWideConsumers;
+  uint32_t j_load = 0;
+  auto issue_next = [&]() -> bool {  // loader warp: tile j_load into its slot
+    const int s = (int)(j_load % S);
+    int go = 1;
+    if (lane == 0) {
+      if (j_load >= (uint32_t)S && !mbar_wait_bounded(&empty[s], ((j_load / S) - 1) & 1)) {
+        atomicExch(err, OMR_NTT_ERR_TIMEOUT);
+        abort_flag = 1;
+      }
+      go = !abort_flag;
+      if (go) slot_tile[s] = j_load;
+    }
+    go = __shfl_sync(0xffffffffu, go, 0);
+    if (!go) return false;
+    wide_issue_load_warp<F, MODE>(&in_map, a, tile_of(j_load), base + s * BB, &full[s], lane);
+    j_load++;
+    return true;
+  };
+  if (loader) {
+    if (lane == 0) {
+      for (int s = 0; s < S; s++) {
+        mbar_init(&full[s], 1);
+        mbar_init(&done[s], 8);
+        mbar_init(&rd[s], 8);
+        mbar_init(&empty[s], 1);
+        slot_tile[s] = 0xffffffffu;
+      }
+      fence_mbar_init();
+      unit_next = 0;
+      abort_flag = 0;
+    }
+    __syncwarp();
+    // the previous pass's output is this one's input (and its input may be
+    // this one's output): every global access of the pass follows the
+    // loader's wait (the storer writes only tiles that were loaded after it)
+    if (lane == 0) {
+      prefetch_tmap(&in_map);
+      prefetch_tmap(&out_map);
+    }
+    grid_dep_wait();
+    while (j_load < njobs && j_load < (uint32_t)S && issue_next()) {
+    }
+  }
+  grid_dep_launch();
+  for (int i = threadIdx.x; i < 15 * 16; i += kWideWsThreads) {
+    const int aa = i / 16 + 1, l = i % 16;
+    tab1[i] = a.roots[(uint32_t)(l * aa) * a.roots_stride];  // omega_256^(l a)
+  }
+  __syncthreads();
+
+  if (loader) {
+    // slot s takes tile j once the store of tile j - S has read it
+    while (j_load < njobs && issue_next()) {
+    }
+    // every issued load has landed before the CTA exits (all of them have
+    // been consumed unless a wait gave up)
+    if (lane == 0)
+      for (uint32_t k = j_load > (uint32_t)S ? j_load - S : 0u; k < j_load; k++)
+        mbar_wait_bounded(&full[k % S], (k / S) & 1);
+    return;
+  }
+  if (warp == kWideConsumers + 1) {
+    // storer: one lane; tiles in order
+    if (lane != 0) return;
+    for (uint32_t j = 0; j < njobs; j++) {
+      const int s = (int)(j % S);
+      if (!mbar_wait_bounded(&done[s], (j / S) & 1)) {
+        atomicExch(err, OMR_NTT_ERR_TIMEOUT);
+        abort_flag = 1;
+      }
+      if (abort_flag) break;
+      wide_issue_store<F, MODE>(&out_map, a, tile_of(j), base + s * BB);
+      if (j + S < njobs) {
+        bulk_wait_read_all();
+        mbar_arrive(&empty[s]);
+      }
+    }
+    bulk_wait_all();
+    return;
+  }
+
+  // consumers
+  for (;;) {
+    uint32_t u = 0;
+    if (lane == 0) u = atomicAdd(&unit_next, 1u);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    const uint32_t j = u >> 3;
+    const int w = (int)(u & 7u);
+    if (j >= njobs || abort_flag) break;
+    const int s = (int)(j % S);
+    const uint32_t par = (j / S) & 1;
+    unsigned char* buf = base + s * BB;
+    bool mine = false;
+    for (unsigned long long i = 0; i < kSpinLimit && !(mine = slot_tile[s] == j); i++) __nanosleep(20);
+    if (!mine || !mbar_wait_bounded(&full[s], par)) {
+      if (lane == 0) {
+        atomicExch(err, OMR_NTT_ERR_TIMEOUT);
+        abort_flag = 1;
+      }
+      break;
+    }
+    uint32_t g, lm;
+    uint64_t lb;
+    tile_coords<F, C>(a, tile_of(j), g, lm, lb);
+    E v[VPU][16];
+    wide_lines<F, MODE, INV, TW>(a, buf, tab1, w, g * C, lm, v);
+    if constexpr (MODE != MODE_COL) {
+      // the rows of the output span every column group's lines: re-lay after
+      // all eight units have read theirs
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&rd[s]);
+      if (!mbar_wait_bounded(&rd[s], par)) {
+        if (lane == 0) {
+          atomicExch(err, OMR_NTT_ERR_TIMEOUT);
+          abort_flag = 1;
+        }
+        break;
+      }
+#pragma unroll
+      for (int bb = 0; bb < 16; bb++) {
+        E x[VPU];
+#pragma unroll
+        for (int c = 0; c < VPU; c++) x[c] = v[c][bb];
+        wide_store_unit<F, true>(buf, (lane & 15) + 16 * bb, w, lane >> 4, x);
+      }
+    }
+    fence_proxy_async();  // this thread's writes become visible to the TMA store
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&done[s]);
   }
 }
 
