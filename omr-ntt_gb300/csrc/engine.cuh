@@ -8,6 +8,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/omr_ntt.h"
@@ -28,6 +29,27 @@ int fail(int status, const std::string& msg);
   } while (0)
 
 inline int word_bytes(int field) { return field == GOLDILOCKS ? 8 : 4; }
+
+// Launch with the programmatic stream-serialisation attribute: the kernel's
+// CTAs may be scheduled while the previous kernel of the stream drains, and
+// wait in griddepcontrol.wait (grid_dep_wait, ntt_pass.cuh) until it has
+// completed.  Every kernel launched this way calls grid_dep_wait() before
+// its first global access.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                       Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 int two_adicity(int field);
 uint64_t modulus(int field);
 bool valid_field(int field);

@@ -32,8 +32,7 @@ int launch_pass_t(const PassArgs<F>& a, uint64_t blocks, cudaStream_t stream) {
   }
   if (blocks == 0) return OMR_NTT_OK;
   if (blocks > 0x7fffffffull) return fail(OMR_NTT_ERR_SIZE, "pass grid too large");
-  ntt_tile_pass<F, LOGT, V, MODE, INV><<<(unsigned)blocks, NT, smem, stream>>>(a);
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(ntt_tile_pass<F, LOGT, V, MODE, INV>, dim3((unsigned)blocks), dim3(NT), smem, stream, a));
   return OMR_NTT_OK;
 }
 
@@ -168,8 +167,7 @@ int launch_tma_k(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (store) failed");
   const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
   const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
-  kern<<<grid, NT, smem, stream>>>(in_map, out_map, a, err);
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(kern, dim3(grid), dim3(NT), smem, stream, in_map, out_map, a, err));
   return OMR_NTT_OK;
 }
 
@@ -228,8 +226,7 @@ int launch_slab_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (slab store) failed");
   const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
   const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
-  kern<<<grid, NT, smem, stream>>>(in_map, out_map, a, err);
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(kern, dim3(grid), dim3(NT), smem, stream, in_map, out_map, a, err));
   return OMR_NTT_OK;
 }
 
@@ -269,13 +266,6 @@ int launch_wide_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
     r = encode_2d(&out_map, F::WORD, a.out, w, 256ull * a.L_b, w, C, 256, sw);
   }
   if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (wide store) failed");
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.stream = stream;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
   if constexpr (F::WORD == 8) {
     // Goldilocks: the warp-specialised form (one CTA per SM, no CTA barrier)
     // is 4-7% faster on GB300 (2^24 0.381 against 0.393 ms, 64 x 2^20 1.33
@@ -292,17 +282,13 @@ int launch_wide_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
       ws_ready[dev & 63] = 1;
     }
     const uint64_t sms = (uint64_t)device_sm_count(dev);
-    cfg.gridDim = dim3((unsigned)(ntiles < sms ? ntiles : sms));
-    cfg.blockDim = dim3(kWideWsThreads);
-    cfg.dynamicSmemBytes = smem_ws;
-    OMR_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern_ws, in_map, out_map, a, err));
+    OMR_CUDA_TRY(launch_pdl(kern_ws, dim3((unsigned)(ntiles < sms ? ntiles : sms)), dim3(kWideWsThreads), smem_ws,
+                            stream, in_map, out_map, a, err));
     return OMR_NTT_OK;
   }
   const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
-  cfg.gridDim = dim3((unsigned)(ntiles < slots ? ntiles : slots));
-  cfg.blockDim = dim3(kWideThreads);
-  cfg.dynamicSmemBytes = smem;
-  OMR_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, in_map, out_map, a, err));
+  OMR_CUDA_TRY(launch_pdl(kern, dim3((unsigned)(ntiles < slots ? ntiles : slots)), dim3(kWideThreads), smem, stream,
+                          in_map, out_map, a, err));
   return OMR_NTT_OK;
 }
 
@@ -395,8 +381,7 @@ int launch_tc_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
   const unsigned grid = (unsigned)(ntiles < slots ? ntiles : slots);
   const typename F::Tw one_tw = F::make_tw(1), r32_tw = F::make_tw((1ull << 32) % F::p64());
-  kern<<<grid, kTcThreads, smem, stream>>>(in_map, out_map, a, bmat, one_tw, r32_tw, err);
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(kern, dim3(grid), dim3(kTcThreads), smem, stream, in_map, out_map, a, bmat, one_tw, r32_tw, err));
   return OMR_NTT_OK;
 }
 

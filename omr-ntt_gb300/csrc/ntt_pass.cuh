@@ -29,6 +29,20 @@
 
 namespace omr {
 
+// Programmatic dependent launch.  Every kernel of the engine is launched with
+// the programmatic stream-serialisation attribute (launch_pdl, engine.cuh), so
+// its CTAs may start while the previous kernel of the stream finishes.
+// griddepcontrol.wait blocks until that kernel has completed and its writes
+// are visible; launch_dependents lets the next kernel start.  A kernel calls
+// grid_dep_wait() before its first global access (its input may be the
+// previous kernel's output, its output that kernel's input).
+OMR_D void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+OMR_D void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+OMR_D void pdl_entry() {
+  grid_dep_wait();
+  grid_dep_launch();
+}
+
 constexpr int kMaxLogT = 12;   // largest line handled by one pass (4096 points)
 constexpr int kTwLoBits = 12;  // two-level four-step twiddle split
 
@@ -340,6 +354,7 @@ OMR_D void all_rounds(const PassArgs<F>& a, typename F::E* s, const typename F::
 template <class F, int LOGT, int V, int MODE, bool INV>
 __global__ void __launch_bounds__(tile_threads<F, LOGT, V>(), tile_min_blocks<F, LOGT, V>())
     ntt_tile_pass(const PassArgs<F> a) {
+  pdl_entry();
   using E = typename F::E;
   constexpr int T = 1 << LOGT;
   constexpr int C = tile_cols<F, V>();

@@ -319,6 +319,7 @@ template <class F, int LOGT, int MODE, bool INV, bool TW>
 __global__ void __launch_bounds__(slab_threads<LOGT>(), (slab_min_blocks<F, LOGT>()))
     ntt_slab_pass(const __grid_constant__ CUtensorMap in_map,
                   const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
+  pdl_entry();
   using Tw = typename F::Tw;
   constexpr int R0 = 1 << slab_r0_log<LOGT>(), C = slab_cols<F>();
   constexpr int NT = slab_threads<LOGT>();

@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
                      const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a,
                      const uint16_t* __restrict__ bmat, typename F::Tw one_tw, typename F::Tw r32_tw,
                      int* err) {
+  pdl_entry();
   static_assert(F::WORD == 4, "32-bit fields only");
   using E = typename F::E;
   using Tw = typename F::Tw;

@@ -45,12 +45,6 @@ OMR_D void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
                "r"(bytes)
                : "memory");
 }
-// Programmatic dependent launch: a pass launched with the programmatic
-// stream-serialisation attribute may start while the previous kernel of the
-// stream finishes; griddepcontrol.wait blocks until that kernel has completed
-// and its writes are visible, launch_dependents lets the next one start.
-OMR_D void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-OMR_D void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 OMR_D void prefetch_tmap(const CUtensorMap* m) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(m)) : "memory");
 }
@@ -388,6 +382,7 @@ template <class F, int LOGT, int C, int NT, int MODE, bool INV, bool TW, int NBU
 __global__ void __launch_bounds__(NT, (tma_min_blocks<F, LOGT, NT, NBUF>()))
     ntt_tile_pass_tma(const __grid_constant__ CUtensorMap in_map,
                       const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
+  pdl_entry();
   using E = typename F::E;
   using Tw = typename F::Tw;
   constexpr size_t BW = tma_buf_words<F, LOGT, C>();

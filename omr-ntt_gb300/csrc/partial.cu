@@ -12,6 +12,7 @@ template <class F>
 __global__ void gather_kernel(const typename F::E* __restrict__ full, uint64_t n, int pattern,
                               uint64_t count, const uint32_t* __restrict__ idx,
                               typename F::E* __restrict__ out) {
+  pdl_entry();
   uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   if (j >= count) return;
   uint64_t k;
@@ -29,6 +30,7 @@ __global__ void gather_kernel(const typename F::E* __restrict__ full, uint64_t n
 template <class F>
 __global__ void colsum_kernel(const typename F::E* __restrict__ x, uint64_t rows, uint64_t cols,
                               uint64_t rows_per_chunk, typename F::E* __restrict__ partial) {
+  pdl_entry();
   using E = typename F::E;
   uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   uint64_t chunk = blockIdx.y;
@@ -52,8 +54,7 @@ static int launch_colsum(const typename F::E* x, uint64_t rows, uint64_t cols,
   uint64_t rpc = (rows + nchunks - 1) / nchunks;
   nchunks = (rows + rpc - 1) / rpc;
   dim3 grid((unsigned)col_blocks, (unsigned)nchunks);
-  colsum_kernel<F><<<grid, 256, 0, st>>>(x, rows, cols, rpc, partial);
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(colsum_kernel<F>, grid, dim3(256), 0, st, x, rows, cols, rpc, partial));
   *nchunks_out = nchunks;
   return OMR_NTT_OK;
 }
@@ -67,6 +68,7 @@ template <class F>
 __global__ void __launch_bounds__(256) fold_flat_kernel(const typename F::E* __restrict__ x,
                                                         uint64_t n, uint32_t count,
                                                         typename F::E* __restrict__ partial) {
+  pdl_entry();
   using E = typename F::E;
   __shared__ E red[256];
   const uint64_t stride = (uint64_t)gridDim.x * 256;
@@ -101,6 +103,7 @@ template <class F>
 __global__ void __launch_bounds__(kFoldThreads) fold_vec_kernel(const typename F::E* __restrict__ x,
                                                                 uint64_t n, uint32_t count,
                                                                 typename F::E* __restrict__ partial) {
+  pdl_entry();
   using E = typename F::E;
   constexpr int VW = 16 / F::WORD;
   constexpr int CH = kFoldThreads * VW;  // words per CTA per sweep step
@@ -174,13 +177,13 @@ static int run_fold(omr_ntt_domain_s* d, int sub_plan, uint64_t count, const voi
     const uint64_t m = count / ch > 4 ? count / ch : 4;  // grid stride a multiple of count
     g = g < m ? m : g & ~(m - 1);
     const uint32_t grid = (uint32_t)g;
-    fold_vec_kernel<F><<<grid, kFoldThreads, 0, stream>>>(static_cast<const E*>(in), d->n, (uint32_t)count, part);
-    OMR_CUDA_TRY(cudaGetLastError());
+    OMR_CUDA_TRY(launch_pdl(fold_vec_kernel<F>, dim3(grid), dim3(kFoldThreads), 0, stream, static_cast<const E*>(in), d->n,
+                            (uint32_t)count, part));
     nch = count > ch ? grid / (count / ch) : grid;
   } else if (count <= 4096 && d->n >= 256ull * 1216) {
     const uint32_t grid = 1216;  // 8 CTAs per SM; a multiple of count / 256 for count <= 4096
-    fold_flat_kernel<F><<<grid, 256, 0, stream>>>(static_cast<const E*>(in), d->n, (uint32_t)count, part);
-    OMR_CUDA_TRY(cudaGetLastError());
+    OMR_CUDA_TRY(launch_pdl(fold_flat_kernel<F>, dim3(grid), dim3(256), 0, stream, static_cast<const E*>(in), d->n,
+                            (uint32_t)count, part));
     nch = count >= 256 ? grid / (count / 256) : grid;
   } else {
     rc = launch_colsum<F>(static_cast<const E*>(in), rows, count, part, max_chunks, &nch, stream);
@@ -205,9 +208,8 @@ static int run_gather(omr_ntt_domain_s* d, int plan, int pattern, uint64_t count
   rc = run_transform(d, plan, false, in, full, 1, stream);
   if (rc) return rc;
   unsigned blocks = (unsigned)((count + 255) / 256);
-  gather_kernel<F><<<blocks, 256, 0, stream>>>(static_cast<const E*>(full), d->n, pattern, count,
-                                              indices, static_cast<E*>(out));
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(gather_kernel<F>, dim3(blocks), dim3(256), 0, stream, static_cast<const E*>(full), d->n,
+                          pattern, count, indices, static_cast<E*>(out)));
   return OMR_NTT_OK;
 }
 
@@ -265,9 +267,9 @@ int launch_gather_indices(const void* full, uint64_t n, uint64_t count, const ui
                           void* out, cudaStream_t stream) {
   using E = typename F::E;
   if (count == 0) return OMR_NTT_OK;
-  gather_kernel<F><<<(unsigned)((count + 255) / 256), 256, 0, stream>>>(
-      static_cast<const E*>(full), n, OMR_NTT_PATTERN_INDICES, count, idx, static_cast<E*>(out));
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(gather_kernel<F>, dim3((unsigned)((count + 255) / 256)), dim3(256), 0, stream,
+                          static_cast<const E*>(full), n, (int)OMR_NTT_PATTERN_INDICES, count, idx,
+                          static_cast<E*>(out)));
   return OMR_NTT_OK;
 }
 template int launch_gather_indices<BabyBear>(const void*, uint64_t, uint64_t, const uint32_t*,

@@ -93,6 +93,7 @@ template <class F, int LOGT>
 __global__ void __launch_bounds__(prefix_threads<F, LOGT>(), 2)
     prefix_decomp_kernel(const PassArgs<F> a, uint32_t m, const uint32_t* __restrict__ idx,
                          typename F::E* __restrict__ partial) {
+  pdl_entry();
   using E = typename F::E;
   using Tw = typename F::Tw;
   constexpr int T = 1 << LOGT;
@@ -194,6 +195,7 @@ template <class F>
 __global__ void __launch_bounds__(kReduceThreads)
     reduce_rows_kernel(const typename F::E* __restrict__ partial, uint32_t rows, uint32_t cols,
                        uint32_t cw, typename F::E* __restrict__ out) {
+  pdl_entry();
   using E = typename F::E;
   __shared__ E red[kReduceThreads];
   const uint32_t slices = kReduceThreads / cw;
@@ -228,9 +230,8 @@ inline int launch_reduce_rows(const typename F::E* partial, uint64_t rows, uint6
   uint32_t cw = 1;
   while (cw < 32 && cw < cols) cw <<= 1;
   const unsigned blocks = (unsigned)((cols + cw - 1) / cw);
-  reduce_rows_kernel<F><<<blocks, kReduceThreads, 0, stream>>>(partial, (uint32_t)rows, (uint32_t)cols,
-                                                               cw, out);
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(reduce_rows_kernel<F>, dim3(blocks), dim3(kReduceThreads), 0, stream, partial,
+                          (uint32_t)rows, (uint32_t)cols, cw, out));
   return OMR_NTT_OK;
 }
 
@@ -278,8 +279,7 @@ inline int launch_prefix_t(omr_ntt_domain_s* d, uint32_t m, const uint32_t* idx,
   void* part = nullptr;
   rc = domain_scratch(d, stream, (size_t)grid * m * sizeof(E), &part, 1);
   if (rc) return rc;
-  kern<<<grid, NT, smem, stream>>>(a, m, idx, static_cast<E*>(part));
-  OMR_CUDA_TRY(cudaGetLastError());
+  OMR_CUDA_TRY(launch_pdl(kern, dim3(grid), dim3(NT), smem, stream, a, m, idx, static_cast<E*>(part)));
   return launch_reduce_rows<F>(static_cast<const E*>(part), grid, m, static_cast<E*>(out), stream);
 }
 
