@@ -277,12 +277,12 @@ int launch_wide_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
     if (!ws_ready[dev & 63].load()) {
       OMR_CUDA_TRY(cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ws));
       int occ_ws = 0;
-      OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ws, kern_ws, kWideWsThreads, smem_ws));
+      OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ws, kern_ws, wide_ws_threads<F>(), smem_ws));
       if (occ_ws < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "wide pass does not fit on an SM");
       ws_ready[dev & 63] = 1;
     }
     const uint64_t sms = (uint64_t)device_sm_count(dev);
-    OMR_CUDA_TRY(launch_pdl(kern_ws, dim3((unsigned)(ntiles < sms ? ntiles : sms)), dim3(kWideWsThreads), smem_ws,
+    OMR_CUDA_TRY(launch_pdl(kern_ws, dim3((unsigned)(ntiles < sms ? ntiles : sms)), dim3(wide_ws_threads<F>()), smem_ws,
                             stream, in_map, out_map, a, err));
     return OMR_NTT_OK;
   }

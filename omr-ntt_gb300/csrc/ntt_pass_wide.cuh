@@ -350,8 +350,17 @@ __global__ void __launch_bounds__(kWideThreads, 3)  // shared memory holds three
 // it waits on `full`.  `rd` and `done` are safe without that check, because
 // a unit reaches them only after its tile's load, i.e. after every unit of
 // the slot's previous tile has passed both.
-constexpr int kWideConsumers = 24;
-constexpr int kWideWsThreads = 32 * (kWideConsumers + 2);  // + loader and storer warps
+// 24 consumer warps (72 registers at 832 threads).  For the 32-bit fields
+// the form measured slower than the three-CTA pass with 24 consumers at 72
+// registers and with 22 at 80, so only Goldilocks launches it.
+template <class F>
+constexpr int wide_consumers() {
+  return 24;
+}
+template <class F>
+constexpr int wide_ws_threads() {
+  return 32 * (wide_consumers<F>() + 2);  // + loader and storer warps
+}
 constexpr int kWideSlots = 6;
 
 template <class F>
@@ -360,7 +369,7 @@ constexpr size_t wide_ws_smem_bytes() {
 }
 
 template <class F, int MODE, bool INV, bool TW>
-__global__ void __launch_bounds__(kWideWsThreads, 1)
+__global__ void __launch_bounds__(wide_ws_threads<F>(), 1)
     ntt_wide_ws_pass(const __grid_constant__ CUtensorMap in_map,
                      const __grid_constant__ CUtensorMap out_map, const PassArgs<F> a, int* err) {
   using E = typename F::E;
@@ -384,7 +393,8 @@ __global__ void __launch_bounds__(kWideWsThreads, 1)
 
   // The loader warp sets up the barriers and sends the first loads before
   // anything else, so the copies overlap the table setup.
-  const bool loader = warp == kWideConsumers;
+  constexpr int NC = wide_consumers<F>();
+  const bool loader = warp == NC;
   uint32_t j_load = 0;
   auto issue_next = [&]() -> bool {  // loader warp: tile j_load into its slot
     const int s = (int)(j_load % S);
@@ -429,7 +439,7 @@ __global__ void __launch_bounds__(kWideWsThreads, 1)
     }
   }
   grid_dep_launch();
-  for (int i = threadIdx.x; i < 15 * 16; i += kWideWsThreads) {
+  for (int i = threadIdx.x; i < 15 * 16; i += wide_ws_threads<F>()) {
     const int aa = i / 16 + 1, l = i % 16;
     tab1[i] = a.roots[(uint32_t)(l * aa) * a.roots_stride];  // omega_256^(l a)
   }
@@ -446,7 +456,7 @@ __global__ void __launch_bounds__(kWideWsThreads, 1)
         mbar_wait_bounded(&full[k % S], (k / S) & 1);
     return;
   }
-  if (warp == kWideConsumers + 1) {
+  if (warp == NC + 1) {
     // storer: one lane; tiles in order
     if (lane != 0) return;
     for (uint32_t j = 0; j < njobs; j++) {
