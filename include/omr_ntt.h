@@ -123,7 +123,7 @@ const char *omr_ntt_encoder_name(int encoder);
 int omr_ntt_encoder_supports(int encoder, uint32_t log_n);
 
 /* The plan a full encoder runs for a 2^log_n transform of `field`: each of the
- * reference's algorithms (src/encoders/*.rs) maps to the engine plan family
+ * reference's algorithms (the files under src/encoders/) maps to the engine plan family
  * with its structure -- WinterfellFourStep the balanced two-pass slab plan,
  * Plonky3Radix2LayerSplit the shorter-pass-first split at log2(N) / 2,
  * LambdaBowers the 256-point wide passes, LambdaRadix4 even-length passes,

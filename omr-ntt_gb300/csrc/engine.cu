@@ -553,6 +553,7 @@ int omr_ntt_domain_destroy(omr_ntt_domain_t d) {
   cudaFree(d->tw_lo_i);
   cudaFree(d->tw_hi_i);
   for (auto& kv : d->scratch) cudaFree(kv.second.ptr);
+  for (auto& kv : d->line_tw) cudaFree(kv.second);
   for (auto& kv : d->subs) omr_ntt_domain_destroy(kv.second);
   for (cudaStream_t s : d->host_streams)
     if (s) cudaStreamDestroy(s);

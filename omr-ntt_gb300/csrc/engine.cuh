@@ -8,6 +8,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -139,6 +140,10 @@ struct omr_ntt_domain_s {
   std::map<std::pair<void*, int>, omr::Scratch> scratch;  // keyed by (stream, slot)
   std::vector<omr::PlanShape> plans;
   std::map<uint32_t, omr_ntt_domain_s*> subs;  // smaller domains (same field) for partial paths
+  // [line][k] four-step twiddle tables of 256-point column passes (device),
+  // keyed by (inverse, tw_scale, lines); built on first use
+  std::mutex line_tw_mu;
+  std::map<std::tuple<int, uint64_t, uint32_t>, void*> line_tw;
 };
 
 namespace omr {
@@ -182,8 +187,9 @@ struct DeviceGuard {
   }
 };
 
-// Typed launch of one pass.
+// Typed launch of one pass.  may_alloc = false: use only device tables that
+// already exist (the allocation-free entry point).
 template <class F>
 int launch_pass(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, const void* in,
-                void* out, bool last, cudaStream_t stream);
+                void* out, bool last, cudaStream_t stream, bool may_alloc = true);
 }  // namespace omr

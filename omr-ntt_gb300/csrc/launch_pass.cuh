@@ -505,13 +505,60 @@ int make_pass_args(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, c
   return OMR_NTT_OK;
 }
 
+// The [line][k] four-step twiddle table of a 256-point column pass: entry
+// (line, k) = omega^((line * tw_scale * k) mod N) as F::Tw, line < lines.
+// Built on the host once per (domain, direction, tw_scale, lines) and kept
+// by the domain; with may_alloc = false only an existing table is returned.
+constexpr uint32_t kLineTwMaxLines = 8192;  // 16 MB of 8-byte operands at most
+
+template <class F>
+int line_twiddles(omr_ntt_domain_s* d, bool inverse, uint64_t tw_scale, uint32_t lines, bool may_alloc,
+                  const typename F::Tw** out) {
+  using Tw = typename F::Tw;
+  *out = nullptr;
+  const auto key = std::make_tuple(inverse ? 1 : 0, tw_scale, lines);
+  std::lock_guard<std::mutex> lk(d->line_tw_mu);
+  auto it = d->line_tw.find(key);
+  if (it != d->line_tw.end()) {
+    *out = static_cast<const Tw*>(it->second);
+    return OMR_NTT_OK;
+  }
+  if (!may_alloc) return OMR_NTT_OK;
+  const uint64_t p = F::p64(), w = inverse ? d->omega_inv : d->omega;
+  std::vector<Tw> host((size_t)lines * 256);
+  for (uint32_t line = 0; line < lines; line++) {
+    const uint64_t step = hpowmod(w, ((uint64_t)line * tw_scale) & (d->n - 1), p);
+    uint64_t t = 1;
+    for (int k = 0; k < 256; k++) {
+      host[(size_t)line * 256 + k] = F::make_tw(t);
+      t = hmulmod(t, step, p);
+    }
+  }
+  void* dev = nullptr;
+  const size_t bytes = host.size() * sizeof(Tw);
+  if (cudaMalloc(&dev, bytes) != cudaSuccess) return fail(OMR_NTT_ERR_ALLOC, "line twiddle table allocation failed");
+  if (cudaMemcpy(dev, host.data(), bytes, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(dev);
+    return fail(OMR_NTT_ERR_CUDA, "line twiddle table copy failed");
+  }
+  d->line_tw[key] = dev;
+  *out = static_cast<const Tw*>(dev);
+  return OMR_NTT_OK;
+}
+
 template <class F>
 int launch_pass(const omr_ntt_domain_s* d, const PassDesc& p, bool inverse, const void* in,
-                void* out, bool last, cudaStream_t stream) {
+                void* out, bool last, cudaStream_t stream, bool may_alloc) {
   PassArgs<F> a;
   int rc = make_pass_args<F>(d, p, inverse, in, out, last, &a);
   if (rc) return rc;
   const int variant = effective_variant(F::ID, p.mode, p.logT, p.variant);
+  if (p.twiddle && p.mode == MODE_COL && p.logT == 8 && variant == kWideVariant &&
+      (p.L_m == 1 || p.tw_line_mul_m == 0) && p.L_lo <= kLineTwMaxLines) {
+    // a 256-point wide column pass with few lines: its twiddles as one table
+    rc = line_twiddles<F>(const_cast<omr_ntt_domain_s*>(d), inverse, p.tw_scale, p.L_lo, may_alloc, &a.tw_tab);
+    if (rc) return rc;
+  }
   const int C = tile_cols<F, 0>();
   const uint64_t blocks = p.L_b * (uint64_t)p.L_m * (uint64_t)((p.L_lo + C - 1) / C);
   switch (p.mode) {

@@ -102,7 +102,7 @@ extern "C" int omr_ntt_forward_noalloc(omr_ntt_domain_t d, const void* in, void*
     void* dst = p.out_buf == 1 ? scratch : out;
     const bool last = i + 1 == ps.size();
     int rc = with_field(d->field, [&](auto f) {
-      return launch_pass<decltype(f)>(d, p, false, src, dst, last, st);
+      return launch_pass<decltype(f)>(d, p, false, src, dst, last, st, false);
     });
     if (rc) return rc;
   }

@@ -77,6 +77,10 @@ struct PassArgs {
   uint32_t tw_line_mul_m;
   int has_scale;
   Tw scale;  // N^-1 for inverse transforms
+  // optional: the four-step twiddles of the 256-point column passes as one
+  // table [line][k] (tw_line < 2^13, tw_line_mul_m == 0), replacing the
+  // base * step^q chain with one table operand per output
+  const Tw* tw_tab;
 };
 
 // --------------------------------------------------------------- helpers

@@ -200,7 +200,16 @@ OMR_D void wide_lines(const PassArgs<F>& a, unsigned char* s, const typename F::
 #pragma unroll
   for (int c = 0; c < VPU; c++) dft_reg<F, 4, INV>(v[c]);
   // outputs b = 0..15 are line entries am + 16 b
-  if constexpr (TW) {
+  if (TW && a.tw_tab != nullptr) {
+    // twiddle table [line][k]: one operand per output (tw_line_mul_m == 0)
+#pragma unroll
+    for (int c = 0; c < VPU; c++) {
+      const uint32_t line = llo0 + (uint32_t)(w * (16 / F::WORD) + u * VPU + c);
+      const typename F::Tw* row = a.tw_tab + (size_t)line * 256u + am;
+#pragma unroll
+      for (int b = 0; b < 16; b++) v[c][b] = F::mul_tw(v[c][b], row[16 * b]);
+    }
+  } else if constexpr (TW) {
 #pragma unroll
     for (int c = 0; c < VPU; c++) {
       const uint32_t line = llo0 + (uint32_t)(w * (16 / F::WORD) + u * VPU + c) + lm * a.tw_line_mul_m;

@@ -6,5 +6,5 @@ namespace omr {
 template int launch_pass_dir<BabyBear, MODE_COL, false>(int, int, const PassArgs<BabyBear>&, uint64_t, int*,
                                                      cudaStream_t);
 template int launch_pass<BabyBear>(const omr_ntt_domain_s*, const PassDesc&, bool, const void*, void*,
-                             bool, cudaStream_t);
+                             bool, cudaStream_t, bool);
 }  // namespace omr

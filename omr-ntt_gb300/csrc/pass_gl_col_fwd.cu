@@ -6,5 +6,5 @@ namespace omr {
 template int launch_pass_dir<Goldilocks, MODE_COL, false>(int, int, const PassArgs<Goldilocks>&, uint64_t, int*,
                                                      cudaStream_t);
 template int launch_pass<Goldilocks>(const omr_ntt_domain_s*, const PassDesc&, bool, const void*, void*,
-                             bool, cudaStream_t);
+                             bool, cudaStream_t, bool);
 }  // namespace omr

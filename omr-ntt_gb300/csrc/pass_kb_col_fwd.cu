@@ -6,5 +6,5 @@ namespace omr {
 template int launch_pass_dir<KoalaBear, MODE_COL, false>(int, int, const PassArgs<KoalaBear>&, uint64_t, int*,
                                                      cudaStream_t);
 template int launch_pass<KoalaBear>(const omr_ntt_domain_s*, const PassDesc&, bool, const void*, void*,
-                             bool, cudaStream_t);
+                             bool, cudaStream_t, bool);
 }  // namespace omr
