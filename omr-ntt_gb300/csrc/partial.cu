@@ -253,10 +253,14 @@ int partial_dispatch(omr_ntt_domain_s* d, int pattern, uint64_t count, const uin
   if (planned_partial(d->field, d->log_n, pattern, count, &strategy, &param) == 1 &&
       strategy >= STRAT_DECOMP_ && strategy <= STRAT_GATHER_)
     return run_strategy_t<F>(d, strategy, param, pattern, count, indices, in, out, stream);
-  if (pattern == OMR_NTT_PATTERN_STRIDED && count < n)
+  // built-in rule (timings of the exhaustive tuner on GB300): the fold for
+  // strided sets unless they keep more than 2^16 outputs of at most 8 cosets
+  // (then the full transform + gather); the pruned decomposition for <= 4096
+  // outputs of transforms above 2^20, where it beats the full transform
+  if (pattern == OMR_NTT_PATTERN_STRIDED && count < n && !(count > 65536 && n / count <= 8))
     return run_fold<F>(d, -1, count, in, out, stream);
   if ((pattern == OMR_NTT_PATTERN_PREFIX || pattern == OMR_NTT_PATTERN_INDICES) && count <= 4096 &&
-      count < n && n / count >= 2)
+      count < n && n / count >= 2 && d->log_n > 20)
     return launch_prefix<F>(d, (uint32_t)count, 0, in, out, stream,
                             pattern == OMR_NTT_PATTERN_INDICES ? indices : nullptr);
   return run_gather<F>(d, -1, pattern, count, indices, in, out, stream);

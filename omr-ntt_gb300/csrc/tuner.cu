@@ -247,7 +247,15 @@ static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, ui
 // fields, double-buffered for Goldilocks), else plan 0.
 static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   const auto& plans = plan_table(log_n);
-  if (plans.size() <= 1 || plans[0].split.size() < 2) return 0;
+  if (plans.size() <= 1) return 0;
+  // 2^10..2^12: two passes of short lines on the two-CTA variant (class 10)
+  // beat the one-CTA single pass by 20-90% on GB300 (one CTA per transform
+  // leaves the GPU idle); below 2^10 the single launch stays
+  if (log_n >= 10 && log_n <= 12) {
+    const int p = full_class_plan(log_n, 4 * 2 + 2);
+    if (p >= 0) return p;
+  }
+  if (plans[0].split.size() < 2) return 0;
   if (log_n == 24 || (log_n == 16 && batch >= 8))
     for (int i = 0; i < (int)plans.size(); i++)
       if (plans[i].variant == kWideVariant &&
@@ -258,6 +266,12 @@ static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   if (log_n <= 14 || batch >= 8)
     for (int i = 0; i < (int)plans.size(); i++)
       if (plans[i].variant == kClusterVariant) return i;
+  // Goldilocks 2^15..2^23: the slab pass on the balanced split with one more
+  // pass (class 14)
+  if (field == GOLDILOCKS) {
+    const int p = full_class_plan(log_n, 4 * 3 + 2);
+    if (p >= 0) return p;
+  }
   size_t nsplit = 0;
   for (auto& p : plans)
     if (p.variant == 0) nsplit++;

@@ -204,29 +204,35 @@ GATHER_CLASS = FOLD_CLASS + FULL_CLASSES
 
 def heuristic_class(p) -> int:
     """The class the planner picks without database or network (its built-in
-    rule, tuner.cu heuristic_full_plan and partial.cu partial_dispatch): the
-    wide pass where the transform splits into 256-point passes only (2^24;
-    batches of 2^16), the cluster plan for small or batched 2^13..2^16, else
-    the tuned TMA pass on the balanced split; the decomposition for prefixes
-    and index sets <= 4096, the fold for strided sets, else the gather."""
-    tma_cls = {0: 8, 1: 4}  # BabyBear: two CTAs per SM; Goldilocks: double-buffered
-
+    rule, tuner.cu heuristic_full_plan and partial.cu partial_dispatch): two
+    passes of short lines at 2^10..2^12, the wide pass where the transform
+    splits into 256-point passes only (2^24; batches of 2^16), the cluster
+    plan for small or batched 2^13..2^16, else the TMA two-CTA pass on the
+    balanced split (32-bit fields) or the slab pass with one more pass
+    (Goldilocks); the decomposition for prefixes and index sets of <= 4096
+    outputs above 2^20, the fold for strided sets (but for more than 2^16
+    outputs of at most 8 cosets), else the full transform and a gather."""
     def full_class(log_n, batch):
+        if 10 <= log_n <= 12:
+            return 4 * 2 + 2  # two passes of short lines, TMA two-CTA variant
+        if log_n < 10:
+            return 0  # one launch
         if log_n == 24:
             return 4 * 4 + 2  # wide pass, 256 x 256 x 256 (one pass more than the fewest)
         if log_n == 16 and batch >= 8:
             return 4 * 4 + 0  # wide pass, 256 x 256
         if 13 <= log_n <= 16 and (log_n <= 14 or batch >= 8):
             return 3  # the one-launch cluster plan
-        return tma_cls[p["field"]] if (log_n > 12 and p["field"] in (0, 1)) else 0
+        # BabyBear: TMA two CTAs per SM, balanced; Goldilocks: slab, one more pass
+        return 4 * 3 + 2 if p["field"] == 1 else 4 * 2 + 0
 
     full_cls = full_class(p["log_n"], p["batch"])
     n, s = 1 << p["log_n"], point_count(p)
     if s >= n:
         return full_cls
-    if p["pattern"] == "strided":
+    if p["pattern"] == "strided" and not (p["log_s"] > 16 and p["log_n"] - p["log_s"] <= 3):
         return FOLD_CLASS + full_class(p["log_s"], 1)
-    if p["pattern"] in ("contiguous", "random") and s <= 4096 and n // s >= 2:
+    if p["pattern"] in ("contiguous", "random") and s <= 4096 and n // s >= 2 and p["log_n"] > 20:
         return DECOMP_CLASS
     return GATHER_CLASS + full_class(p["log_n"], 1)  # the gather runs one transform at a time
 
