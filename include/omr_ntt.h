@@ -307,9 +307,10 @@ int omr_ntt_planner_load(const char *path);
 
 /* ---------------------------------------------------------------- learned planner */
 
-/* Plan classes: a fixed vocabulary of 40 plans independent of N (12 full
- * transform pass-split x kernel classes, 4 prefix decomposition line lengths,
- * 12 strided-fold sub-plan classes, 12 full-then-gather classes).
+/* Plan classes: a fixed vocabulary of 64 plans independent of N (20 full
+ * transform classes: 5 pass kernels x 4 split kinds, class 3 standing for the
+ * one-launch cluster plan; 4 decomposition line lengths for prefixes and
+ * index sets; 20 strided-fold sub-plan classes; 20 full-then-gather classes).
  * omr_ntt_plan_class_candidate maps class `cls` of a planning point to its
  * concrete candidate (returns 1) or reports it not applicable (0). */
 int omr_ntt_plan_class_count(void);

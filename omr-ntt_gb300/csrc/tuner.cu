@@ -239,12 +239,13 @@ static bool db_lookup(int field, uint32_t log_n, uint64_t batch, int pattern, ui
   return true;
 }
 
-// Built-in heuristic (measured on GB300): the wide pass where a transform
-// splits into 256-point passes only (2^24 = 256^3, and batches of 2^16 =
-// 256^2; one 2^16 transform is latency bound and takes the cluster plan),
-// the one-launch cluster plan for small or batched 2^13..2^16 transforms,
-// else the TMA pass on the balanced split (two CTAs per SM for the 32-bit
-// fields, double-buffered for Goldilocks), else plan 0.
+// Built-in heuristic (from the exhaustive tuner's timings on GB300): two
+// passes of short lines at 2^10..2^12, the wide pass where a transform splits
+// into 256-point passes only (2^24 = 256^3, and batches of 2^16 = 256^2; one
+// 2^16 transform is latency bound and takes the cluster plan), the one-launch
+// cluster plan for small or batched 2^13..2^16 transforms, else the slab pass
+// with one more pass than the fewest (Goldilocks) or the TMA two-CTA pass on
+// the balanced split (32-bit fields), else plan 0.
 static int heuristic_full_plan(int field, uint32_t log_n, uint64_t batch) {
   const auto& plans = plan_table(log_n);
   if (plans.size() <= 1) return 0;

@@ -244,13 +244,20 @@ def regret(T, best, choice):
 
 DATA_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "data")
 DEFAULT_NETWORK = os.path.join(DATA_DIR, "planner_mlp.bin")
+DEFAULT_DB = os.path.join(DATA_DIR, "planner_full.db")
 _default = None
 
 
-def install_default(path: str = DEFAULT_NETWORK):
+def install_default(path: str = DEFAULT_NETWORK, db: str | None = DEFAULT_DB):
     """Load the network trained on GB300 and make it the planner's learned
-    selector (plan = -1 and the partial entry points then use it)."""
+    selector (plan = -1 and the partial entry points then use it), and load
+    the database of exhaustively tuned full-transform plans (`tune_full`),
+    which the planner consults before the network."""
     global _default
+    if db and os.path.exists(db):
+        n = lib().omr_ntt_planner_load(db.encode())
+        if n < 0:
+            check(n)
     h = ctypes.c_void_p()
     check(lib().omr_ntt_mlp_load(path.encode(), ctypes.byref(h)))
     check(lib().omr_ntt_mlp_install(h))

@@ -3,6 +3,7 @@ the persisted planner database."""
 import ctypes
 import os
 
+import omr_ntt
 from omr_ntt import _lib
 from omr_ntt.fields import BabyBear, Goldilocks
 
@@ -69,3 +70,27 @@ def test_encoder_plan_families_are_distinct():
     # one-pass sizes and the partial encoders
     assert E.WinterfellFourStep().plan(BabyBear, 12) == E.ArkRadix2().plan(BabyBear, 12)
     assert L.omr_ntt_encoder_plan(7, 0, 20) < 0 and L.omr_ntt_encoder_plan(4, 0, 21) < 0
+
+
+def test_shipped_full_transform_db():
+    """The database of exhaustively tuned full-transform plans that
+    planner.install_default() loads: one entry per field, log2 N in [6, 24]
+    and batch in (1, 8, 64, 512) within 2^26 words, each a valid plan id of
+    its size (the wide 256^3 plan at 2^24 for both fields)."""
+    from omr_ntt import planner
+    from omr_ntt.tune_full import shapes
+
+    L.omr_ntt_planner_clear()
+    try:
+        n = L.omr_ntt_planner_load(planner.DEFAULT_DB.encode())
+        want = list(shapes(6, 24))
+        assert n == len(want) == 256
+        s, p = ctypes.c_int(), ctypes.c_int()
+        for f, log_n, batch in want:
+            assert L.omr_ntt_planner_get(f.id, log_n, batch, -1, 0, ctypes.byref(s), ctypes.byref(p)) == 1
+            assert s.value == 0 and 0 <= p.value < omr_ntt.plan_count(f, log_n), (f.name, log_n, batch)
+        for f in (BabyBear, Goldilocks):
+            assert L.omr_ntt_planner_get(f.id, 24, 1, -1, 0, ctypes.byref(s), ctypes.byref(p)) == 1
+            assert omr_ntt.plan_describe(f, 24, p.value) == "four-step 256x256x256 wide"
+    finally:
+        L.omr_ntt_planner_clear()
