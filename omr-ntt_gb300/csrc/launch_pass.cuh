@@ -237,21 +237,10 @@ int launch_wide_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   constexpr bool TW = MODE == MODE_COL;
   constexpr int C = wide_cols<F>();
   if (a.L_lo % C || !tma_geometry_ok<F>(a, 8, MODE) || (a.tw_lo != nullptr) != TW) return 1;
-  constexpr size_t smem = wide_smem_bytes<F>();
-  static_assert(smem <= kMaxDynSmem, "wide pass does not fit in shared memory");
-  auto kern = ntt_wide_pass<F, MODE, INV, TW>;
-  static std::atomic<int> occ_cache[64];
-  int dev = 0;
-  cudaGetDevice(&dev);
-  int occ = occ_cache[dev & 63].load();
-  if (occ == 0) {
-    OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWideThreads, smem));
-    if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "wide pass does not fit on an SM");
-    occ_cache[dev & 63] = occ;
-  }
   const uint64_t ntiles = a.L_b * (uint64_t)a.L_m * (a.L_lo / C);
   if (ntiles == 0) return OMR_NTT_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
   CUtensorMap in_map, out_map;
   memset(&in_map, 0, sizeof(in_map));
   CUresult r;
@@ -268,27 +257,38 @@ int launch_wide_t(const PassArgs<F>& a, int* err, cudaStream_t stream) {
   if (r != CUDA_SUCCESS) return fail(OMR_NTT_ERR_CUDA, "cuTensorMapEncodeTiled (wide store) failed");
   if constexpr (F::WORD == 8) {
     // Goldilocks: the warp-specialised form (one CTA per SM, no CTA barrier)
-    // is 4-7% faster on GB300 (2^24 0.381 against 0.393 ms, 64 x 2^20 1.33
-    // against 1.41 ms); for the 32-bit fields it is 8% slower at 2^24
-    constexpr size_t smem_ws = wide_ws_smem_bytes<F>();
-    static_assert(smem_ws <= kMaxDynSmem, "warp-specialised wide pass does not fit in shared memory");
-    auto kern_ws = ntt_wide_ws_pass<F, MODE, INV, TW>;
-    static std::atomic<int> ws_ready[64];
-    if (!ws_ready[dev & 63].load()) {
-      OMR_CUDA_TRY(cudaFuncSetAttribute(kern_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_ws));
-      int occ_ws = 0;
-      OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ws, kern_ws, wide_ws_threads<F>(), smem_ws));
-      if (occ_ws < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "wide pass does not fit on an SM");
-      ws_ready[dev & 63] = 1;
+    // is 4-7% faster on GB300 (2^24 0.378 against 0.400 ms, 64 x 2^20 1.33
+    // against 1.41 ms); for the 32-bit fields it is 8-10% slower at 2^24
+    constexpr size_t smem = wide_ws_smem_bytes<F>();
+    static_assert(smem <= kMaxDynSmem, "warp-specialised wide pass does not fit in shared memory");
+    auto kern = ntt_wide_ws_pass<F, MODE, INV, TW>;
+    static std::atomic<int> ready[64];
+    if (!ready[dev & 63].load()) {
+      OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int occ = 0;
+      OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, wide_ws_threads<F>(), smem));
+      if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "wide pass does not fit on an SM");
+      ready[dev & 63] = 1;
     }
     const uint64_t sms = (uint64_t)device_sm_count(dev);
-    OMR_CUDA_TRY(launch_pdl(kern_ws, dim3((unsigned)(ntiles < sms ? ntiles : sms)), dim3(wide_ws_threads<F>()), smem_ws,
+    OMR_CUDA_TRY(launch_pdl(kern, dim3((unsigned)(ntiles < sms ? ntiles : sms)), dim3(wide_ws_threads<F>()), smem,
                             stream, in_map, out_map, a, err));
-    return OMR_NTT_OK;
+  } else {
+    constexpr size_t smem = wide_smem_bytes<F>();
+    static_assert(smem <= kMaxDynSmem, "wide pass does not fit in shared memory");
+    auto kern = ntt_wide_pass<F, MODE, INV, TW>;
+    static std::atomic<int> occ_cache[64];
+    int occ = occ_cache[dev & 63].load();
+    if (occ == 0) {
+      OMR_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      OMR_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWideThreads, smem));
+      if (occ < 1) return fail(OMR_NTT_ERR_INVALID_ARGUMENT, "wide pass does not fit on an SM");
+      occ_cache[dev & 63] = occ;
+    }
+    const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
+    OMR_CUDA_TRY(launch_pdl(kern, dim3((unsigned)(ntiles < slots ? ntiles : slots)), dim3(kWideThreads), smem,
+                            stream, in_map, out_map, a, err));
   }
-  const uint64_t slots = (uint64_t)device_sm_count(dev) * occ;
-  OMR_CUDA_TRY(launch_pdl(kern, dim3((unsigned)(ntiles < slots ? ntiles : slots)), dim3(kWideThreads), smem, stream,
-                          in_map, out_map, a, err));
   return OMR_NTT_OK;
 }
 
