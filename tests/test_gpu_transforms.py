@@ -115,6 +115,43 @@ def test_batch_64_of_2_20(oracle, field):
     assert np.array_equal(to_host(yd, field.dtype), x)
 
 
+@pytest.mark.parametrize("field", [BabyBear, Goldilocks, KoalaBear], ids=lambda f: f.name)
+@pytest.mark.parametrize("log_n,batch", [(16, 2), (20, 3), (16, 8)])  # sizes with a 256-point pass
+def test_wide_column_pass_twiddle_tables(oracle, field, log_n, batch):
+    """Every wide plan whose 256-point column pass takes its four-step
+    twiddles from the domain's [line][k] table (at most 8192 lines), in
+    batches, forward and inverse (the two directions use separate tables),
+    against the oracle -- and the same words from the allocation-free entry
+    point, which reuses the tables the first call built."""
+    import ctypes
+
+    import torch
+
+    from omr_ntt import _lib
+
+    n = 1 << log_n
+    d = NttDomain(field, n)
+    x = gen_input_seeded(field, n * batch, 91 + log_n)
+    exp = oracle.forward(field.id, x, batch=batch)
+    wide = [p for p in range(omr_ntt.plan_count(field, log_n))
+            if omr_ntt.plan_describe(field, log_n, p).endswith(" wide")]
+    assert wide
+    for plan in wide:
+        xd = to_dev(x)
+        yd = torch.empty_like(xd)
+        omr_ntt.forward(d, xd, plan=plan, out=yd, batch=batch)
+        assert np.array_equal(to_host(yd, field.dtype), exp), (log_n, plan)
+        omr_ntt.inverse(d, yd, plan=plan, batch=batch)
+        assert np.array_equal(to_host(yd, field.dtype), x), (log_n, plan)
+    if n * batch * field.word_bytes <= 16 << 20:
+        out = torch.empty_like(xd)
+        sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _lib.check(_lib.lib().omr_ntt_forward_noalloc(d.handle, ctypes.c_void_p(xd.data_ptr()),
+                                                      ctypes.c_void_p(out.data_ptr()), batch, sp))
+        torch.cuda.synchronize()
+        assert np.array_equal(to_host(out, field.dtype), exp)
+
+
 @pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
 def test_out_of_place_and_in_place_agree(oracle, field):
     n = 1 << 14
