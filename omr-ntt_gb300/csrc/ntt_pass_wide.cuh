@@ -12,7 +12,8 @@
 //
 //   * column passes: one 2-D TMA box [C lines x 256 rows] per tile, landed
 //     with the 128-byte swizzle (16-byte chunk ch of row r at chunk
-//     ch ^ (r mod 8)), so every lane access below is conflict-free;
+//     ch ^ (r mod 8)), so that with the lane mapping of wide_lane_l /
+//     wide_lane_u every access below is conflict-free;
 //     row passes: one 1-D bulk copy per line into a padded line-major layout;
 //   * warp w owns the 16-byte column group w (4 or 2 lines); its lanes run
 //     the 256-point transforms of those lines as 16 x 16 (radix-16 round,
@@ -58,6 +59,17 @@ constexpr size_t wide_smem_bytes() {
 
 // 128-byte-swizzled row layout: byte of (row r, 16-byte chunk ch, offset o)
 OMR_D int wide_sw(int r, int ch, int o) { return r * 128 + ((ch ^ (r & 7)) << 4) + o; }
+
+// Lane -> (l, u) of the line transforms: l = lane bits 0-2 and 4, u = bit 3.
+// The shared-memory pipe serves 8-byte accesses a half-warp at a time, so
+// each half-warp (lanes 0-15, 16-31) holds the eight values of l mod 8 --
+// eight distinct chunk positions of the swizzle, as rows r = l + 16 m,
+// 16 a + (l ^ a) and a + 16 b all have r mod 8 = l mod 8 (^ a) -- and both
+// units u: 16 distinct 8-byte slots, one wavefront per half-warp.  (l = lane
+// & 15, u = lane >> 4 put rows r and r + 8 of one unit into the same
+// half-warp: a two-way conflict on every access.)
+OMR_D int wide_lane_l(int lane) { return (lane & 7) | ((lane >> 1) & 8); }
+OMR_D int wide_lane_u(int lane) { return (lane >> 3) & 1; }
 
 // The column unit u (8 bytes) of column group w, row r.
 template <class F, bool ROWS_LAYOUT>
@@ -153,7 +165,7 @@ OMR_D void wide_issue_load_warp(const CUtensorMap* map, const PassArgs<F>& a, ui
 }
 
 // One warp: the 256-point transforms of column group w.  The results are
-// left in registers, v[c][b] = line entry a + 16 b (a = lane & 15); column
+// left in registers, v[c][b] = line entry a + 16 b (a = wide_lane_l(lane)); column
 // passes also write them to the swizzled rows in place, row passes re-lay
 // them as rows after a CTA barrier (their lines span every column group).
 template <class F, int MODE, bool INV, bool TW>
@@ -163,7 +175,7 @@ OMR_D void wide_lines(const PassArgs<F>& a, unsigned char* s, const typename F::
   constexpr int VPU = slab_vpu<F>();
   constexpr bool ROWS = MODE == MODE_COL;
   const int lane = threadIdx.x & 31;
-  const int l = lane & 15, u = lane >> 4;
+  const int l = wide_lane_l(lane), u = wide_lane_u(lane);
 #pragma unroll
   for (int m = 0; m < 16; m++) {
     E x[VPU];
@@ -315,7 +327,7 @@ __global__ void __launch_bounds__(kWideThreads, 3)  // shared memory holds three
         E x[VPU];
 #pragma unroll
         for (int c = 0; c < VPU; c++) x[c] = v[c][bb];
-        wide_store_unit<F, true>(s, (lane & 15) + 16 * bb, warp, lane >> 4, x);
+        wide_store_unit<F, true>(s, wide_lane_l(lane) + 16 * bb, warp, wide_lane_u(lane), x);
       }
     }
     fence_proxy_async();  // this thread's writes become visible to the TMA store
@@ -527,7 +539,7 @@ __global__ void __launch_bounds__(wide_ws_threads<F>(), 1)
         E x[VPU];
 #pragma unroll
         for (int c = 0; c < VPU; c++) x[c] = v[c][bb];
-        wide_store_unit<F, true>(buf, (lane & 15) + 16 * bb, w, lane >> 4, x);
+        wide_store_unit<F, true>(buf, wide_lane_l(lane) + 16 * bb, w, wide_lane_u(lane), x);
       }
     }
     fence_proxy_async();  // this thread's writes become visible to the TMA store
