@@ -235,7 +235,17 @@ OMR_D void slab_rounds12(const PassArgs<F>& a, unsigned char* s, const typename 
   using E = typename F::E;
   constexpr int R0 = 1 << slab_r0_log<LOGT>(), VPU = slab_vpu<F>();
   const int lane = threadIdx.x & 31;
-  const int l = lane & 15, u = lane >> 4;
+  // 16-byte rows (r * 16 + 8 u: column passes, and every pass's final
+  // staging) take 8-byte accesses a half-warp at a time, so each half-warp
+  // holds the eight values of l mod 8 and both units (l = lane bits 0-2 and 4,
+  // u = bit 3): every access of the rounds below (rows l + 16 m, 16 a + (l ^ a),
+  // 16 l + (k ^ l), a + 16 b) lands on 16 distinct 8-byte slots.  The
+  // line-major rounds of row passes are conflict-free with it for 4-byte
+  // words; for 8-byte (Goldilocks) words there l = lane & 15, u = lane >> 4
+  // is, so those row passes keep that assignment.
+  constexpr bool kHalfWarp = MODE == MODE_COL || F::WORD == 4;
+  const int l = kHalfWarp ? ((lane & 7) | ((lane >> 1) & 8)) : (lane & 15);
+  const int u = kHalfWarp ? ((lane >> 3) & 1) : (lane >> 4);
   E v[VPU][16];
   // round 1: lane l transforms rows l + 16 m (m < 16) of its column unit
 #pragma unroll
