@@ -19,7 +19,9 @@
 //     the 256-point transforms of those lines as 16 x 16 (radix-16 round,
 //     twiddle omega_256^(l a), exchange through the warp's own column group
 //     with an XOR swizzle and __syncwarp, radix-16 round), then the four-step
-//     twiddle (column passes) and the inverse scale;
+//     twiddle (column passes: one operand per output from the domain's
+//     [line][k] table when the pass has at most 8192 lines, else a
+//     base * step^q chain) and the inverse scale;
 //   * the results go back as 128-byte rows k = a + 16 b (natural order; a
 //     256-point line needs no output permutation) and one 2-D TMA store
 //     writes the tile;
@@ -27,6 +29,9 @@
 // Per tile that is one CTA barrier for column passes (every warp's results
 // in the buffer before the store) and two for row passes (the lines are
 // re-laid as rows in place).  Waits are bounded as in the other passes.
+// Thread 0 waits on the previous kernel of the stream (programmatic
+// dependent launch) before the first load.  Goldilocks runs the
+// warp-specialised form at the end of this file.
 //
 // The 256-point line transform is the same 16 x 16 split as the slab pass
 // (ntt_pass_slab.cuh), i.e. the reference's four-step decomposition
