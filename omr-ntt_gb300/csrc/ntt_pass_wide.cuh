@@ -50,7 +50,11 @@ constexpr int wide_cols() {
 constexpr int kWideThreads = 256;  // 8 warps: one per 16-byte column group
 template <class F>
 constexpr int wide_line_bytes() {
-  return 256 * F::WORD + 32;  // row-pass line-major layout (padded)
+  // row-pass line-major layout, padded so that the lines of a unit sit on
+  // other banks: lines 2u + c of the 32-bit fields 8 banks apart (4-byte
+  // accesses, a whole warp at a time), Goldilocks lines 2w + u 16 banks apart
+  // (8-byte accesses, a half-warp of eight l and two u at a time)
+  return 256 * F::WORD + (F::WORD == 8 ? 64 : 32);
 }
 template <class F>
 constexpr int wide_buf_bytes() {  // a 1024-byte multiple (128-byte swizzle atoms)
