@@ -152,6 +152,42 @@ def test_wide_column_pass_twiddle_tables(oracle, field, log_n, batch):
         assert np.array_equal(to_host(out, field.dtype), exp)
 
 
+@pytest.mark.parametrize("field,log_n,plan_word", [(BabyBear, 24, " wide"), (Goldilocks, 20, " wide"),
+                                                   (BabyBear, 22, " slab"), (BabyBear, 16, " tma2cta")])
+def test_graph_captured_transform(oracle, field, log_n, plan_word):
+    """Transforms captured into a CUDA graph (after a warm-up call has built
+    the domain's scratch and twiddle tables) and replayed: every pass kernel
+    is launched with the programmatic stream-serialisation attribute, which
+    capture turns into programmatic graph edges; replays are bit-exact."""
+    import torch
+
+    n = 1 << log_n
+    d = NttDomain(field, n)
+    plan = next(p for p in range(omr_ntt.plan_count(field, log_n))
+                if omr_ntt.plan_describe(field, log_n, p).endswith(plan_word))
+    x = gen_input_seeded(field, n, 123 + log_n)
+    xd = to_dev(x)
+    yd = torch.empty_like(xd)
+    zd = torch.empty_like(xd)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        omr_ntt.forward(d, xd, plan=plan, out=yd)  # warm-up: allocations happen here
+        omr_ntt.inverse(d, yd, plan=plan, out=zd)
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        omr_ntt.forward(d, xd, plan=plan, out=yd)
+        omr_ntt.inverse(d, yd, plan=plan, out=zd)
+    yd.zero_()
+    zd.zero_()
+    torch.cuda.synchronize()
+    for _ in range(2):
+        g.replay()
+    torch.cuda.synchronize()
+    assert np.array_equal(to_host(yd, field.dtype), oracle.forward(field.id, x))
+    assert np.array_equal(to_host(zd, field.dtype), x)
+
+
 @pytest.mark.parametrize("field", [BabyBear, Goldilocks], ids=lambda f: f.name)
 def test_out_of_place_and_in_place_agree(oracle, field):
     n = 1 << 14
